@@ -1,0 +1,387 @@
+"""Benchmark of the GB300 direction-optimizing BFS (GTEPS, harmonic mean over sources).
+
+One step = one direction-optimizing BFS from each of the workload's sources
+(the reference's SourcePicker sequence, -n 64), on a synthetic graph built
+exactly as the reference builds it.  The graph (CSR in HBM) is far larger
+than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--graph g22|g26|u26|...]
+    python bench.py --impl reference ...   # the reference's CPU path, same metric
+
+Multi-GPU runs are replicas (weak scaling): each rank owns its own slice of the
+source sequence and its own copy of the graph; nothing is exchanged but the
+final timings.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRAPHS = {
+    # name: (scale, degree, uniform)
+    "g20": (20, 16, False), "g22": (22, 16, False), "g24": (24, 16, False),
+    "g26": (26, 16, False), "u22": (22, 16, True), "u26": (26, 16, True),
+}
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbbfs", choices=["gbbfs", "reference"])
+    ap.add_argument("--graph", default="g22", choices=sorted(GRAPHS))
+    ap.add_argument("--sources", type=int, default=64)
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0,
+                    help="bound on the CPU-baseline sample")
+    return ap.parse_args(argv)
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def replica_sources(all_sources, rank, world, per_rank):
+    """Rank r's sources: the r-th block of `per_rank` picks of the sequence."""
+    return all_sources[rank * per_rank:(rank + 1) * per_rank]
+
+
+def combine_replicas(per_rank):
+    """Whole-job value from per-rank (hmean GTEPS, timed seconds) pairs.
+
+    Each replica contributes its own harmonic-mean rate for the fraction of
+    the job's wall time (max over ranks) it was busy; at N=1 this is the
+    rank's harmonic mean.
+    """
+    t_max = max(t for _, t in per_rank)
+    return sum(v * (t / t_max) for v, t in per_rank), t_max
+
+
+def hmean_gteps(edges, seconds):
+    """Harmonic mean over searches of (edges / 2) / t."""
+    inv = sum(t / (e / 2.0) for e, t in zip(edges, seconds) if e > 0)
+    cnt = sum(1 for e in edges if e > 0)
+    return (cnt / inv) * 1e-9 if inv > 0 else 0.0
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def step_alg_bytes(n, step, prev_count):
+    """Algorithmic bytes of one step (the byte model of the BFS path)."""
+    k = step["kind"]
+    if k == "td":
+        return 20 * prev_count + 8 * step["edges"] + 8 * step["count"]
+    if k == "bu":
+        return 4 * n + n // 4 + 8 * step["unvisited"] + 4 * step["edges"] + 4 * step["count"]
+    if k == "e":
+        return 4 * step["count"] + n // 8
+    return n // 8 + 4 * step["count"]
+
+
+def load_traffic(graph, kernel):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(graph, {}).get(kernel)
+
+
+def cpu_port_sample(off, nbr, sources, budget_s, threads):
+    """The oracle port of the reference's OpenMP DOBFS on the host cores."""
+    from oracle import oracle as O
+    deg = np.diff(off)
+    edges, secs = [], []
+    t0 = time.time()
+    for s in sources:
+        parent, _, _, t = O.dobfs(off, nbr, int(s), threads=threads, want_steps=False)
+        edges.append(int(deg[parent >= 0].sum()))
+        secs.append(t)
+        if time.time() - t0 > budget_s:
+            break
+    return edges, secs
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    scale, degree, uniform = GRAPHS[args.graph]
+    off, nbr = O.build_synthetic(scale, degree, uniform)
+    sources = O.source_picker(off, args.sources)
+    threads = os.cpu_count() or 1
+    per_step = max(1, min(args.sources, 16 if scale >= 25 else args.sources))
+    deg = np.diff(off)
+    reached = {}
+    for _ in range(args.warmup):
+        for s in sources[:per_step]:
+            parent, _, _, _ = O.dobfs(off, nbr, int(s), threads=threads, want_steps=False)
+            reached[int(s)] = int(deg[parent >= 0].sum())
+    edges, secs, step_times = [], [], []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        chunk = [sources[(k * per_step + i) % len(sources)] for i in range(per_step)]
+        for s in chunk:
+            parent, _, _, t = O.dobfs(off, nbr, int(s), threads=threads, want_steps=False)
+            edges.append(int(deg[parent >= 0].sum()))
+            secs.append(t)
+        step_times.append(time.perf_counter() - t0)
+    value = hmean_gteps(edges, secs)
+    sample = "%d of the %d sources per step on %s (n=%d, m_dir=%d)" % (
+        per_step, args.sources, args.graph, len(off) - 1, len(nbr))
+    line = {
+        "impl": "reference", "metric": "GTEPS (harmonic mean over sources)", "value": value,
+        "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(step_times) / len(step_times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": workload_config(args, len(off) - 1, len(nbr)),
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config(args, n, m):
+    scale, degree, uniform = GRAPHS[args.graph]
+    return {"workload": "%s-%d degree %d direction-optimizing BFS, %d SourcePicker sources"
+                        % ("uniform" if uniform else "kronecker", scale, degree, args.sources),
+            "graph": args.graph, "num_nodes": n, "num_edges_directed": m,
+            "alpha": 15, "beta": 18, "sources_per_step": args.sources,
+            "parallelism": "replicas" if args.gpus > 1 else "single-gpu",
+            "l2": "inputs larger than L2: CSR %.2f GB" % ((4 * m + 8 * (n + 1)) / 1e9)}
+
+
+def run_gbbfs(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    else:
+        tdist = None
+        torch.cuda.set_device(0)
+    from dist_mem_gapbs_gb300 import _build, gbbfs
+    _build.build()
+    scale, degree, uniform = GRAPHS[args.graph]
+    t0 = time.time()
+    off, nbr = gbbfs.make_graph(scale, degree, uniform)
+    build_s = time.time() - t0
+    n, m = len(off) - 1, len(nbr)
+    all_sources = gbbfs.pick_sources(off, args.sources * world)
+    sources = [int(s) for s in replica_sources(all_sources, rank, world, args.sources)]
+    deg = np.diff(off)
+    g = gbbfs.Graph(off, nbr)
+
+    # Untimed instrumented pass: per-source reached edges and per-step byte counts.
+    info = {}
+    for s in sources:
+        st = gbbfs.bfs_device(g, s, stats=True, instrument=True)
+        parent = np.empty(n, np.int32)
+        gbbfs.results(g, parent)
+        info[s] = dict(edges=int(deg[parent >= 0].sum()), steps=st.steps)
+
+    def one_step(record):
+        for s in sources:
+            st = gbbfs.bfs_device(g, s, stats=True)
+            if record is not None:
+                record.append((s, st))
+
+    for _ in range(args.warmup):
+        one_step(None)
+
+    records = []
+    if tdist is not None:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            one_step(records)
+        torch.cuda.synchronize()
+        elapsed = time.perf_counter() - t0
+    if tdist is not None:
+        tdist.barrier()
+    edges = [info[s]["edges"] for s, _ in records]
+    secs = [st.device_ms * 1e-3 for _, st in records]
+    my_value = hmean_gteps(edges, secs)
+    busy = sum(secs)
+
+    # Kernel shares and the roofline of the dominant kernel (device events
+    # around every step kernel, on the library's stream).
+    kind_time = {"init": 0.0, "td": 0.0, "bu": 0.0, "e": 0.0, "c": 0.0}
+    kind_bytes = {"init": 0, "td": 0, "bu": 0, "e": 0, "c": 0}
+    kind_launch = {"init": 0, "td": 0, "bu": 0, "e": 0, "c": 0}
+    for s, st in records:
+        kind_time["init"] += st.init_seconds
+        kind_bytes["init"] += 12 * n
+        kind_launch["init"] += 1
+        prev = 1
+        for step, ref in zip(st.steps, info[s]["steps"]):
+            kind_time[step["kind"]] += step["seconds"]
+            kind_bytes[step["kind"]] += step_alg_bytes(n, ref, prev)
+            kind_launch[step["kind"]] += 1
+            prev = ref["count"]
+    launches = sum(kind_launch.values())
+    kernel_names = {"init": "k_init", "td": "k_td", "bu": "k_bu", "e": "k_q2b", "c": "k_b2q"}
+    dom = max(kind_time, key=lambda k: kind_time[k])
+    peak, peak_kind = measured_peaks()
+    achieved = kind_bytes[dom] / kind_time[dom] / 1e9 if kind_time[dom] > 0 else 0.0
+    traffic = load_traffic(args.graph, kernel_names[dom])
+
+    # End to end through the public call: source in, parent array back in
+    # pinned host memory, every search.
+    pinned = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    host_parent = pinned.numpy()
+    e2e_secs, e2e_edges = [], []
+    for s in sources:
+        t1 = time.perf_counter()
+        gbbfs.DOBFS(g, s, parent_out=host_parent)
+        e2e_secs.append(time.perf_counter() - t1)
+        e2e_edges.append(info[s]["edges"])
+    e2e_value = hmean_gteps(e2e_edges, e2e_secs)
+
+    if tdist is not None:
+        t = torch.tensor([my_value, elapsed, e2e_value], dtype=torch.float64, device="cuda")
+        allv = [torch.zeros_like(t) for _ in range(world)]
+        tdist.all_gather(allv, t)
+        per_rank = [(float(x[0]), float(x[1])) for x in allv]
+        value, t_max = combine_replicas(per_rank)
+        e2e_total, _ = combine_replicas([(float(x[2]), float(x[1])) for x in allv])
+    else:
+        value, t_max = my_value, elapsed
+        e2e_total = e2e_value
+
+    if rank == 0:
+        cpu = None
+        threads = os.cpu_count() or 1
+        c_edges, c_secs = cpu_port_sample(off, nbr, sources, args.cpu_budget_s, threads)
+        cpu = {"value": hmean_gteps(c_edges, c_secs), "unit": "GTEPS", "cores": threads,
+               "kind": "port",
+               "sample": "%d sources of the workload, oracle port of the reference's OpenMP "
+                         "DOBFS" % len(c_secs)}
+        share = {k: kind_time[k] / max(1e-12, sum(kind_time.values())) for k in kind_time}
+        line = {
+            "metric": "GTEPS (harmonic mean over sources)", "value": value, "unit": "GTEPS",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": workload_config(args, n, m),
+            "roofline": {"bound": "hbm", "kernel": kernel_names[dom], "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": traffic,
+                         "alg_bytes_per_launch": kind_bytes[dom] / max(1, kind_launch[dom]),
+                         "launch_ms": 1e3 * kind_time[dom] / max(1, kind_launch[dom])},
+            "kernel_share": share,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_total, "unit": "GTEPS", "h2d_bytes_per_step": 4 * len(sources),
+                    "d2h_bytes_per_step": 4 * n * len(sources)},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+            "device_busy_s": busy, "graph_build_s": build_s,
+        }
+        print(json.dumps(line))
+    g.close()
+    if tdist is not None:
+        tdist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gbbfs(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

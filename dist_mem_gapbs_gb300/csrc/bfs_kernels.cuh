@@ -1,0 +1,429 @@
+// CUDA kernels of the direction-optimizing BFS (sm_103a).
+//
+// Data layout in HBM (n vertices, W = ceil(n/32) bitmap words):
+//   off      OffT[n+1]   CSR offsets; OffT = uint32 when m_dir < 2^32, else uint64
+//   nbr      int32[m]    sorted neighbour lists (in == out: the graph is symmetric)
+//   iso      u32[W]      bit set for degree-0 vertices and ids >= n
+//   visited  u32[W]      bit set once a vertex has a parent
+//   front    u32[W]      bottom-up frontier; next u32[W] the one being built
+//   parent   int32[32W]  the BFS tree, -1 while unvisited
+//   depth    int32[32W]  BFS depth, -1 while unvisited (optional)
+//   qv/qs    frontier queue: vertex ids and the exclusive prefix sum of their
+//            out-degrees, in queue order (two of each, current and next)
+//
+// A bitmap word w covers vertices [32w, 32w+32); in bottom-up steps one warp
+// owns a word at a time, so next/visited/parent of that range have exactly
+// one writer and need no atomics (the reference's per-PE vertex ranges of
+// src/partition.h:69-161, one level finer).
+#pragma once
+
+#include "bfs_common.cuh"
+
+namespace gbbfs {
+
+// ---------------------------------------------------------------------------
+// InitParent (src/bfs.cc:131-140, gapbs-verify/bfs.cc:114-120) fused with the
+// frontier set-up of DOBFS (src/bfs.cc:150-159): parent = -1 everywhere, the
+// source its own parent, visited = iso | {source}, front = 0, queue = {source}.
+// The reference keeps -out_degree in parent for unvisited vertices so that
+// scout_count can sum it; here the degree is read from the offsets at claim
+// time instead, which keeps the init a pure store stream.
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads)
+k_init(int64_t n, int64_t W, const OffT* __restrict__ off, const uint32_t* __restrict__ iso,
+       uint32_t* __restrict__ visited, uint32_t* __restrict__ front,
+       int32_t* __restrict__ parent, int32_t* __restrict__ depth, int32_t source,
+       int32_t* __restrict__ qv0, OffT* __restrict__ qs0, DevCounters* __restrict__ ctr,
+       int shift) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // parent / depth: 8 int32 per thread-iteration (32-byte stores).
+  const int64_t nvec = W * 4;  // 32W ints / 8
+  const int64_t src_vec = source >> 3;
+  const int src_lane = source & 7;
+  auto put = [](int4 v, int lane, int val) {
+    v.x = lane == 0 ? val : v.x;
+    v.y = lane == 1 ? val : v.y;
+    v.z = lane == 2 ? val : v.z;
+    v.w = lane == 3 ? val : v.w;
+    return v;
+  };
+  const int4 neg = make_int4(-1, -1, -1, -1);
+  for (int64_t i = tid; i < nvec; i += stride) {
+    const bool here = i == src_vec;
+    const int la = here ? src_lane : -1, lb = here ? src_lane - 4 : -1;
+    reinterpret_cast<int4*>(parent)[2 * i] = put(neg, la, source);
+    reinterpret_cast<int4*>(parent)[2 * i + 1] = put(neg, lb, source);
+    if (depth) {
+      reinterpret_cast<int4*>(depth)[2 * i] = put(neg, la, 0);
+      reinterpret_cast<int4*>(depth)[2 * i + 1] = put(neg, lb, 0);
+    }
+  }
+  const int64_t src_word = source >> 5;
+  for (int64_t w = tid; w < W; w += stride) {
+    uint32_t v = iso[w];
+    if (w == src_word) v |= 1u << (source & 31);
+    visited[w] = v;
+    front[w] = 0;
+  }
+  if (tid == 0) {
+    qv0[0] = source;
+    qs0[0] = 0;
+    const unsigned long long deg = (unsigned long long)(off[source + 1] - off[source]);
+    ctr->qpacked[0] = (1ull << shift) | deg;
+    ctr->qpacked[1] = 0;
+    ctr->awake = 0;
+    ctr->scanned = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Top-down step: TDStep (gapbs-verify/bfs.cc:67-89, src/bfs.cc:81-100).
+//
+// The frontier's edges are numbered 0..E-1 through the degree prefix sum qs.
+// Each warp takes one contiguous span of edge numbers, finds the queue entry
+// of its first edge by binary search, then walks the span 32 edges at a time
+// (one edge per lane, consecutive lanes on consecutive neighbours: coalesced
+// loads) while sliding a 32-entry window over the queue.  So a hub of degree
+// 10^6 is spread over many warps and 32 degree-1 vertices fill one warp.
+//
+// A neighbour v is claimed by atomicOr on its visited bit (the reference's
+// compare_and_swap on parent[v]); the winner writes parent[v] = u and appends
+// v to the next queue.  scout_count (the summed degrees of claimed vertices)
+// falls out of the packed queue counter.  Claims are staged per warp in
+// shared memory and appended with one atomic per 256 claims.
+constexpr int kTdStage = 256;
+
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads)
+k_td(const OffT* __restrict__ off, const int32_t* __restrict__ nbr, uint32_t* visited,
+     int32_t* __restrict__ parent, int32_t* __restrict__ depth,
+     const int32_t* __restrict__ qv, const OffT* __restrict__ qs,
+     int32_t* __restrict__ qv_out, OffT* __restrict__ qs_out,
+     DevCounters* __restrict__ ctr, int cur, int shift, int level) {
+  __shared__ int32_t st_v[kWarpsPerCta][kTdStage];
+  __shared__ OffT st_d[kWarpsPerCta][kTdStage];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const unsigned long long packed = ctr->qpacked[cur];
+  const int64_t F = (int64_t)(packed >> shift);
+  const unsigned long long emask = (1ull << shift) - 1;
+  const uint64_t E = packed & emask;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t nchunks = (E + 31) >> 5;
+  const uint64_t per = (nchunks + nwarps - 1) / nwarps;
+  const uint64_t c_begin = warp * per;
+  const uint64_t c_end = c_begin + per < nchunks ? c_begin + per : nchunks;
+  int staged = 0;
+
+  auto flush = [&]() {
+    // One atomic for the whole stage: (count << shift) + summed degrees.
+    OffT red = 0;
+    for (int i = lane; i < staged; i += 32) red += st_d[wib][i];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) red += shfl(red, lane ^ o);
+    unsigned long long base = 0;
+    if (lane == 0)
+      base = atomicAdd(&ctr->qpacked[cur ^ 1],
+                       ((unsigned long long)staged << shift) + (unsigned long long)red);
+    base = shfl(base, 0);
+    const uint64_t qbase = base >> shift;
+    OffT ebase = (OffT)(base & emask);
+    for (int i0 = 0; i0 < staged; i0 += 32) {
+      const int i = i0 + lane;
+      const OffT d = i < staged ? st_d[wib][i] : 0;
+      const OffT inc = warp_inclusive_sum(d, lane);
+      if (i < staged) {
+        qv_out[qbase + i] = st_v[wib][i];
+        qs_out[qbase + i] = ebase + inc - d;
+      }
+      ebase += shfl(inc, 31);
+    }
+    __syncwarp();
+    staged = 0;
+  };
+
+  if (c_begin < c_end) {
+    uint64_t e0 = c_begin << 5;
+    // Last queue entry whose first edge is <= e0.
+    int64_t lo = 0, hi = F - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if ((uint64_t)qs[mid] <= e0) lo = mid; else hi = mid - 1;
+    }
+    int64_t i0 = lo;
+    for (uint64_t c = c_begin; c < c_end; c++, e0 += 32) {
+      const int64_t ij = i0 + lane;
+      uint64_t sj = ~0ull;
+      int32_t uj = 0;
+      uint64_t rj = 0;
+      if (ij < F) {
+        sj = (uint64_t)qs[ij];
+        uj = qv[ij];
+        rj = (uint64_t)off[uj];
+      }
+      // Bit p set <=> a window entry starts at edge e0 + p (entry i0 covers e0).
+      unsigned mybit = 0;
+      if (lane == 0) mybit = 1u;
+      else if (ij < F && sj < e0 + 32) mybit = 1u << (unsigned)(sj - e0);
+      const unsigned starts = __reduce_or_sync(kFull, mybit);
+      const int k = __popc(starts & (kFull >> (31 - lane))) - 1;
+      const int32_t u = __shfl_sync(kFull, uj, k);
+      const uint64_t s = shfl(sj, k);
+      const uint64_t r = shfl(rj, k);
+      const uint64_t e = e0 + lane;
+      bool claimed = false;
+      int32_t v = 0;
+      OffT dv = 0;
+      if (e < E) {
+        v = __ldg(nbr + (r + (e - s)));
+        const uint32_t bit = 1u << (v & 31);
+        uint32_t* wp = visited + (v >> 5);
+        if (!(__ldcg(wp) & bit)) {
+          const uint32_t old = atomicOr(wp, bit);
+          if (!(old & bit)) {
+            claimed = true;
+            parent[v] = u;
+            if (depth) depth[v] = level;
+            dv = __ldg(off + v + 1) - __ldg(off + v);
+          }
+        }
+      }
+      const unsigned cm = __ballot_sync(kFull, claimed);
+      if (cm) {
+        const int cnt = __popc(cm);
+        if (staged + cnt > kTdStage) flush();
+        if (claimed) {
+          const int slot = staged + __popc(cm & ((1u << lane) - 1));
+          st_v[wib][slot] = v;
+          st_d[wib][slot] = dv;
+        }
+        staged += cnt;
+        __syncwarp();
+      }
+      // Advance to the entry that covers edge e0 + 32.  The window holds 32
+      // entries; when all of them start at or before e0 + 32, entry i0 + 32
+      // may start exactly there.
+      const unsigned le = __ballot_sync(kFull, lane == 0 || (ij < F && sj <= e0 + 32));
+      int adv = __popc(le) - 1;
+      if (le == kFull && i0 + 32 < F && (uint64_t)qs[i0 + 32] == e0 + 32) adv = 32;
+      i0 += adv;
+    }
+  }
+  if (staged) flush();
+}
+
+// ---------------------------------------------------------------------------
+// QueueToBitmap (gapbs-verify/bfs.cc:92-98, src/bfs.cc:104-112): set the bit
+// of every queue entry in `front` (all zero on entry).
+__global__ void __launch_bounds__(kThreads)
+k_q2b(const int32_t* __restrict__ qv, const DevCounters* __restrict__ ctr, int cur, int shift,
+      uint32_t* front) {
+  const int64_t F = (int64_t)(ctr->qpacked[cur] >> shift);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = qv[i];
+    atomicOr(front + (v >> 5), 1u << (v & 31));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bottom-up step: BUStep (gapbs-verify/bfs.cc:46-64, src/bfs.cc:57-78).
+//
+// One warp per bitmap word.  Every unvisited vertex u of the word looks for
+// the FIRST neighbour (in sorted order) whose front bit is set, as the
+// reference does, so bottom-up parents equal the reference's.  Each lane first
+// probes the first kProbe neighbours of its own vertex; vertices still open
+// after that are then scanned by the whole warp, 32 neighbours per ballot,
+// with early exit.  The warp writes next[w] and visited[w] whole.
+constexpr int kProbe = 4;
+
+template <typename OffT, bool kInstrument>
+__global__ void __launch_bounds__(kThreads, 4)
+k_bu(int64_t W, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
+     uint32_t* __restrict__ visited, int32_t* __restrict__ parent, int32_t* __restrict__ depth,
+     const uint32_t* __restrict__ front, uint32_t* __restrict__ next,
+     DevCounters* __restrict__ ctr, int level) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned long long awake = 0, scanned = 0;
+  for (int64_t w = warp; w < W; w += nwarps) {
+    const uint32_t vis = visited[w];
+    const uint32_t unv = ~vis;
+    uint32_t claimed_mask = 0;
+    if (unv) {
+      const int64_t u = (w << 5) + lane;
+      const bool mine = (unv >> lane) & 1u;
+      uint64_t rs = 0, re = 0;
+      if (mine) {
+        rs = (uint64_t)off[u];
+        re = (uint64_t)off[u + 1];
+      }
+      uint64_t pos = rs;
+      int32_t par = -1;
+      bool found = false;
+      if (mine) {
+        const uint64_t stop = re < rs + kProbe ? re : rs + kProbe;
+        for (; pos < stop; pos++) {
+          const int32_t v = __ldg(nbr + pos);
+          if ((__ldg(front + (v >> 5)) >> (v & 31)) & 1u) {
+            par = v;
+            found = true;
+            break;
+          }
+        }
+      }
+      unsigned long long my_scan = 0;
+      if (kInstrument && mine) my_scan = found ? pos - rs + 1 : pos - rs;
+      unsigned pend = __ballot_sync(kFull, mine && !found && pos < re);
+      while (pend) {
+        const int src = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const uint64_t b = shfl(pos, src);
+        const uint64_t e = shfl(re, src);
+        int32_t hit = -1;
+        uint64_t hitpos = e;
+        for (uint64_t base = b; base < e; base += 32) {
+          const uint64_t idx = base + lane;
+          bool h = false;
+          int32_t v = 0;
+          if (idx < e) {
+            v = __ldg(nbr + idx);
+            h = (__ldg(front + (v >> 5)) >> (v & 31)) & 1u;
+          }
+          const unsigned hb = __ballot_sync(kFull, h);
+          if (hb) {
+            const int first = __ffs(hb) - 1;
+            hit = __shfl_sync(kFull, v, first);
+            hitpos = base + first;
+            break;
+          }
+        }
+        if (lane == src) {
+          if (hit >= 0) {
+            found = true;
+            par = hit;
+          }
+          if (kInstrument) my_scan += (hit >= 0 ? hitpos + 1 : e) - b;
+        }
+      }
+      if (found) {
+        parent[u] = par;
+        if (depth) depth[u] = level;
+      }
+      claimed_mask = __ballot_sync(kFull, found);
+      if (kInstrument) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) my_scan += __shfl_xor_sync(kFull, my_scan, o);
+        scanned += my_scan;
+      }
+      if (lane == 0 && claimed_mask) visited[w] = vis | claimed_mask;
+      awake += __popc(claimed_mask);
+    }
+    if (lane == 0) next[w] = claimed_mask;
+  }
+  // One atomic per CTA.
+  __shared__ unsigned long long red[2][kWarpsPerCta];
+  if (lane == 0) {
+    red[0][threadIdx.x >> 5] = awake;
+    red[1][threadIdx.x >> 5] = scanned;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long a = 0, s = 0;
+    for (int i = 0; i < kWarpsPerCta; i++) {
+      a += red[0][i];
+      s += red[1][i];
+    }
+    if (a) atomicAdd(&ctr->awake, a);
+    if (kInstrument && s) atomicAdd(&ctr->scanned, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// BitmapToQueue (gapbs-verify/bfs.cc:100-112, src/bfs.cc:115-125): every set
+// bit of `front` becomes a queue entry (with its degree prefix) and `front`
+// is cleared on the way, so it is all-zero for the next QueueToBitmap.
+// Thread per word; one atomic per CTA-iteration.
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads)
+k_b2q(int64_t W, const OffT* __restrict__ off, uint32_t* __restrict__ front,
+      int32_t* __restrict__ qv_out, OffT* __restrict__ qs_out, DevCounters* __restrict__ ctr,
+      int dst, int shift) {
+  __shared__ unsigned long long warp_tot[kWarpsPerCta];
+  __shared__ unsigned long long cta_base;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const unsigned long long emask = (1ull << shift) - 1;
+  const int64_t span = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t w0 = (int64_t)blockIdx.x * blockDim.x; w0 < W; w0 += span) {
+    const int64_t w = w0 + threadIdx.x;
+    uint32_t bits = 0;
+    if (w < W) {
+      bits = front[w];
+      if (bits) front[w] = 0;
+    }
+    unsigned long long degsum = 0;
+    for (uint32_t b = bits; b; b &= b - 1) {
+      const int64_t u = (w << 5) + (__ffs(b) - 1);
+      degsum += (unsigned long long)(off[u + 1] - off[u]);
+    }
+    // packed (count, degree sum) per thread; inclusive scan over the CTA
+    const unsigned long long mine = ((unsigned long long)__popc(bits) << shift) + degsum;
+    const unsigned long long inc = warp_inclusive_sum(mine, lane);
+    if (lane == 31) warp_tot[wib] = inc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long t = 0;
+      for (int i = 0; i < kWarpsPerCta; i++) {
+        const unsigned long long x = warp_tot[i];
+        warp_tot[i] = t;
+        t += x;
+      }
+      cta_base = t ? atomicAdd(&ctr->qpacked[dst], t) : 0;
+    }
+    __syncthreads();
+    if (bits) {
+      const unsigned long long at = cta_base + warp_tot[wib] + inc - mine;
+      uint64_t qpos = at >> shift;
+      uint64_t epos = at & emask;
+      for (uint32_t b = bits; b; b &= b - 1) {
+        const int64_t u = (w << 5) + (__ffs(b) - 1);
+        qv_out[qpos] = (int32_t)u;
+        qs_out[qpos] = (OffT)epos;
+        qpos++;
+        epos += (uint64_t)(off[u + 1] - off[u]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Graph upload helpers.
+template <typename OffT>
+__global__ void k_narrow_offsets(const int64_t* __restrict__ in, OffT* __restrict__ out,
+                                 int64_t count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (OffT)in[i];
+}
+
+// iso bit = degree 0 or id >= n: never visited, never scanned.
+template <typename OffT>
+__global__ void k_iso_mask(int64_t n, int64_t W, const OffT* __restrict__ off,
+                           uint32_t* __restrict__ iso) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < W;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    for (int b = 0; b < 32; b++) {
+      const int64_t u = (w << 5) + b;
+      if (u >= n || off[u + 1] == off[u]) m |= 1u << b;
+    }
+    iso[w] = m;
+  }
+}
+
+}  // namespace gbbfs

@@ -1,0 +1,158 @@
+// Graph file input/output for the host side of the BFS path.
+//
+// Formats follow the reference's Reader / Writer: ".sg" serialized graphs
+// (src/writer.h:39-69, src/reader.h:291-345), ".el" and ".wel" edge lists and
+// DIMACS ".gr" files (gapbs-verify/reader.h:49-84).  Edge lists go through
+// gbbfs_build_csr, the same construction the synthetic graphs use.
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbbfs.h"
+
+namespace {
+
+std::string Suffix(const std::string& path) {
+  const size_t p = path.rfind('.');
+  return p == std::string::npos ? std::string() : path.substr(p);
+}
+
+// Read whitespace-separated integers; `per_edge` values per record, of which
+// the first two are the endpoints.  For ".gr", only lines starting with 'a'.
+int ReadEdgeText(const std::string& path, bool dimacs, int per_edge,
+                 std::vector<int32_t>* el) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return GBBFS_ERR_IO;
+  std::vector<char> buf(1 << 20);
+  std::string line;
+  char* lp = nullptr;
+  size_t cap = 0;
+  ssize_t len;
+  int rc = GBBFS_OK;
+  while ((len = getline(&lp, &cap, f)) >= 0) {
+    const char* p = lp;
+    while (*p == ' ' || *p == '\t') p++;
+    if (*p == '\n' || *p == '\0' || *p == '\r') continue;
+    if (dimacs) {
+      if (*p != 'a') continue;
+      p++;
+    } else if (*p == '#' || *p == '%') {
+      continue;
+    }
+    long long vals[3] = {0, 0, 0};
+    int got = 0;
+    char* end = nullptr;
+    for (; got < per_edge; got++) {
+      vals[got] = strtoll(p, &end, 10);
+      if (end == p) break;
+      p = end;
+    }
+    if (got < 2) {
+      rc = GBBFS_ERR_IO;
+      break;
+    }
+    long long u = vals[0], v = vals[1];
+    if (dimacs) {
+      u -= 1;
+      v -= 1;
+    }
+    if (u < 0 || v < 0 || u > INT32_MAX || v > INT32_MAX) {
+      rc = GBBFS_ERR_IO;
+      break;
+    }
+    el->push_back(static_cast<int32_t>(u));
+    el->push_back(static_cast<int32_t>(v));
+  }
+  free(lp);
+  fclose(f);
+  return rc;
+}
+
+int ReadSG(const std::string& path, int64_t** offsets_out, int32_t** neigh_out,
+           int64_t* n_out, int64_t* m_out) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return GBBFS_ERR_IO;
+  unsigned char directed = 0;
+  int64_t m = 0, n = 0;
+  if (fread(&directed, 1, 1, f) != 1 || fread(&m, 8, 1, f) != 1 || fread(&n, 8, 1, f) != 1 ||
+      n <= 0 || n > INT32_MAX || m < 0) {
+    fclose(f);
+    return GBBFS_ERR_IO;
+  }
+  if (directed) {
+    fclose(f);
+    return GBBFS_ERR_ARG;  // directed CSR is outside this engine
+  }
+  int64_t* off = static_cast<int64_t*>(malloc(sizeof(int64_t) * (n + 1)));
+  int32_t* nbr = static_cast<int32_t*>(malloc(sizeof(int32_t) * (m > 0 ? m : 1)));
+  if (!off || !nbr) {
+    free(off);
+    free(nbr);
+    fclose(f);
+    return GBBFS_ERR_NOMEM;
+  }
+  bool ok = fread(off, sizeof(int64_t), n + 1, f) == static_cast<size_t>(n + 1) &&
+            (m == 0 || fread(nbr, sizeof(int32_t), m, f) == static_cast<size_t>(m));
+  fclose(f);
+  // The offsets written by the reference are relative to the first vertex.
+  ok = ok && off[0] == 0 && off[n] == m;
+  for (int64_t i = 0; ok && i < n; i++) ok = off[i] <= off[i + 1];
+  for (int64_t e = 0; ok && e < m; e++) ok = nbr[e] >= 0 && nbr[e] < n;
+  if (!ok) {
+    free(off);
+    free(nbr);
+    return GBBFS_ERR_IO;
+  }
+  *offsets_out = off;
+  *neigh_out = nbr;
+  *n_out = n;
+  *m_out = m;
+  return GBBFS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
+                     int32_t** neigh_out, int64_t* n_out, int64_t* m_dir_out) {
+  if (!path || !offsets_out || !neigh_out || !n_out || !m_dir_out) return GBBFS_ERR_ARG;
+  const std::string p(path), suf = Suffix(p);
+  if (suf == ".sg") return ReadSG(p, offsets_out, neigh_out, n_out, m_dir_out);
+  std::vector<int32_t> el;
+  int rc;
+  if (suf == ".el")
+    rc = ReadEdgeText(p, false, 2, &el);
+  else if (suf == ".wel")
+    rc = ReadEdgeText(p, false, 3, &el);
+  else if (suf == ".gr")
+    rc = ReadEdgeText(p, true, 3, &el);
+  else
+    return GBBFS_ERR_ARG;
+  if (rc != GBBFS_OK) return rc;
+  if (!symmetrize) return GBBFS_ERR_ARG;  // directed graphs are outside this engine
+  if (el.empty()) return GBBFS_ERR_IO;
+  return gbbfs_build_csr(el.data(), static_cast<int64_t>(el.size() / 2), -1, offsets_out,
+                         neigh_out, n_out, m_dir_out);
+}
+
+int gbbfs_write_sg(const char* path, const int64_t* offsets, const int32_t* neigh, int64_t n,
+                   int64_t m_dir) {
+  if (!path || !offsets || n <= 0 || m_dir < 0 || (m_dir > 0 && !neigh)) return GBBFS_ERR_ARG;
+  FILE* f = fopen(path, "wb");
+  if (!f) return GBBFS_ERR_IO;
+  const unsigned char directed = 0;
+  bool ok = fwrite(&directed, 1, 1, f) == 1 && fwrite(&m_dir, 8, 1, f) == 1 &&
+            fwrite(&n, 8, 1, f) == 1 &&
+            fwrite(offsets, sizeof(int64_t), n + 1, f) == static_cast<size_t>(n + 1) &&
+            (m_dir == 0 ||
+             fwrite(neigh, sizeof(int32_t), m_dir, f) == static_cast<size_t>(m_dir));
+  if (fclose(f) != 0) ok = false;
+  return ok ? GBBFS_OK : GBBFS_ERR_IO;
+}
+
+}  // extern "C"

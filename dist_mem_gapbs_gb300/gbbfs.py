@@ -1,0 +1,309 @@
+"""Python mirror of the reference's BFS interface over the C ABI (include/gbbfs.h).
+
+Names follow the reference so that tests read like its own usage:
+
+* :func:`make_graph` — ``Builder(cli).MakeGraph()`` for ``-g/-u <scale> -k <degree>``
+  or ``-f <file>`` (src/builder.h:314-338);
+* :class:`Graph` — the CSR graph, resident in HBM (src/graph.h ``CSRGraph``);
+* :class:`SourcePicker` — ``SourcePicker::PickNext`` (src/benchmark.h:49-88);
+* :func:`DOBFS` — the direction-optimizing BFS kernel functor
+  (src/bfs.cc:142-188);
+* :func:`write_bfs_output` — the ``bfs_output.txt`` writer (src/bfs.cc:213-235).
+
+The native library is required: there is no CPU fallback, and every call
+raises :class:`GbbfsError` with the library's status when it fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgbbfs.so")
+CLI_PATH = os.path.join(_HERE, "_lib", "bfs_gpu")
+
+OK, ERR_ARG, ERR_NOMEM, ERR_CUDA, ERR_TIMEOUT, ERR_BOUNDS, ERR_STATE, ERR_IO = range(8)
+STEP_TD, STEP_E, STEP_BU, STEP_C = 1, 2, 3, 4
+STEP_NAME = {STEP_TD: "td", STEP_E: "e", STEP_BU: "bu", STEP_C: "c"}
+
+# Every symbol include/gbbfs.h declares (the tests check the library exports them).
+EXPORTS = (
+    "gbbfs_graph_create", "gbbfs_graph_destroy", "gbbfs_graph_info", "gbbfs_bfs",
+    "gbbfs_bfs_device", "gbbfs_results", "gbbfs_result_device_ptrs", "gbbfs_strerror",
+    "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
+    "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
+    "gbbfs_append_bfs_output",
+)
+
+
+class GbbfsError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        detail = ""
+        if _lib is not None:
+            detail = _lib.gbbfs_last_error().decode()
+            name = _lib.gbbfs_strerror(status).decode()
+        else:
+            name = str(status)
+        super().__init__("%s: %s%s" % (what, name, (" (%s)" % detail) if detail else ""))
+
+
+class Step(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("level", ctypes.c_int32),
+                ("count", ctypes.c_int64), ("edges", ctypes.c_int64),
+                ("unvisited", ctypes.c_int64), ("seconds", ctypes.c_double)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.POINTER(Step)), ("max_steps", ctypes.c_int32),
+                ("instrument", ctypes.c_int32), ("num_steps", ctypes.c_int32),
+                ("levels", ctypes.c_int32), ("device_ms", ctypes.c_double),
+                ("init_seconds", ctypes.c_double), ("reached", ctypes.c_int64),
+                ("alg_bytes", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libgbbfs.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libgbbfs.so is not built (%s); run __graft_entry__.build()"
+                              % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        P, i64, i32, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int
+        PP = ctypes.POINTER(ctypes.c_void_p)
+        sig = {
+            "gbbfs_graph_create": (I, [P, P, i64, i64, PP]),
+            "gbbfs_graph_destroy": (I, [P]),
+            "gbbfs_graph_info": (I, [P, P, P, P]),
+            "gbbfs_bfs": (I, [P, i32, I, I, P, P, P]),
+            "gbbfs_bfs_device": (I, [P, i32, I, I, I, P]),
+            "gbbfs_results": (I, [P, P, P]),
+            "gbbfs_result_device_ptrs": (I, [P, PP, PP]),
+            "gbbfs_strerror": (ctypes.c_char_p, [I]),
+            "gbbfs_last_error": (ctypes.c_char_p, []),
+            "gbbfs_generate": (I, [I, I, I, PP, PP, P, P]),
+            "gbbfs_free_host": (None, [P]),
+            "gbbfs_generate_edges": (I, [I, I, I, PP, P]),
+            "gbbfs_build_csr": (I, [P, i64, i64, PP, PP, P, P]),
+            "gbbfs_read_graph": (I, [ctypes.c_char_p, I, PP, PP, P, P]),
+            "gbbfs_write_sg": (I, [ctypes.c_char_p, P, P, i64, i64]),
+            "gbbfs_pick_sources": (I, [P, i64, i64, I, P]),
+            "gbbfs_append_bfs_output": (I, [ctypes.c_char_p, P, i64]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _check(rc, what):
+    if rc != OK:
+        raise GbbfsError(rc, what)
+
+
+def _take_csr(po, pn, n, m):
+    L = lib()
+    off = np.ctypeslib.as_array(ctypes.cast(po, ctypes.POINTER(ctypes.c_int64)),
+                                shape=(n + 1,)).copy()
+    nbr = np.ctypeslib.as_array(ctypes.cast(pn, ctypes.POINTER(ctypes.c_int32)),
+                                shape=(max(m, 1),))[:m].copy()
+    L.gbbfs_free_host(po)
+    L.gbbfs_free_host(pn)
+    return off, nbr
+
+
+def make_graph(scale=None, degree=16, uniform=False, filename=None, symmetrize=False):
+    """Host CSR (offsets int64[n+1], neigh int32[m]) as Builder::MakeGraph builds it."""
+    L = lib()
+    po, pn = ctypes.c_void_p(), ctypes.c_void_p()
+    n, m = ctypes.c_int64(), ctypes.c_int64()
+    if filename is not None:
+        rc = L.gbbfs_read_graph(os.fsencode(filename), 1 if symmetrize else 0, ctypes.byref(po),
+                                ctypes.byref(pn), ctypes.byref(n), ctypes.byref(m))
+    else:
+        rc = L.gbbfs_generate(int(scale), int(degree), 1 if uniform else 0, ctypes.byref(po),
+                              ctypes.byref(pn), ctypes.byref(n), ctypes.byref(m))
+    _check(rc, "make_graph")
+    return _take_csr(po, pn, n.value, m.value)
+
+
+def build_csr(edges, num_nodes=-1):
+    """Symmetrized, squished CSR of an (E, 2) int32 edge list."""
+    L = lib()
+    el = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+    po, pn = ctypes.c_void_p(), ctypes.c_void_p()
+    n, m = ctypes.c_int64(), ctypes.c_int64()
+    _check(L.gbbfs_build_csr(_p(el), len(el), int(num_nodes), ctypes.byref(po), ctypes.byref(pn),
+                             ctypes.byref(n), ctypes.byref(m)), "build_csr")
+    return _take_csr(po, pn, n.value, m.value)
+
+
+def write_sg(path, offsets, neigh):
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    nbr = np.ascontiguousarray(neigh, dtype=np.int32)
+    _check(lib().gbbfs_write_sg(os.fsencode(path), _p(off), _p(nbr), len(off) - 1, len(nbr)),
+           "write_sg")
+
+
+class SourcePicker:
+    """SourcePicker (src/benchmark.h:49-88): the same sequence of sources."""
+
+    def __init__(self, offsets, given_source=-1):
+        self._off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._given = int(given_source)
+        self._taken = 0
+
+    def take(self, count):
+        """The next `count` picks, as int32 array."""
+        total = self._taken + count
+        out = np.empty(max(total, 1), dtype=np.int32)
+        _check(lib().gbbfs_pick_sources(_p(self._off), len(self._off) - 1, self._given,
+                                        total, _p(out)), "pick_sources")
+        self._taken = total
+        return out[total - count:total]
+
+    def PickNext(self):
+        return int(self.take(1)[0])
+
+
+def pick_sources(offsets, count, given=-1):
+    return SourcePicker(offsets, given).take(count)
+
+
+class Graph:
+    """A CSR graph resident in HBM (one gbbfs_graph handle)."""
+
+    def __init__(self, offsets, neigh):
+        L = lib()
+        self._off = np.ascontiguousarray(offsets, dtype=np.int64)
+        nbr = np.ascontiguousarray(neigh, dtype=np.int32)
+        self.n = len(self._off) - 1
+        self.m = len(nbr)
+        h = ctypes.c_void_p()
+        _check(L.gbbfs_graph_create(_p(self._off), _p(nbr) if self.m else None, self.n, self.m,
+                                    ctypes.byref(h)), "graph_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise GbbfsError(ERR_STATE, "graph closed")
+        return self._h
+
+    def num_nodes(self):
+        return self.n
+
+    def num_edges_directed(self):
+        return self.m
+
+    def num_edges(self):
+        return self.m // 2
+
+    def out_degree(self, v):
+        return int(self._off[v + 1] - self._off[v])
+
+    @property
+    def offsets(self):
+        return self._off
+
+    def device_bytes(self):
+        b = ctypes.c_int64()
+        _check(lib().gbbfs_graph_info(self.handle, None, None, ctypes.byref(b)), "graph_info")
+        return b.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            lib().gbbfs_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class SearchStats:
+    """Result of the stats block of one search."""
+
+    def __init__(self, st, steps):
+        self.device_ms = st.device_ms
+        self.init_seconds = st.init_seconds
+        self.levels = st.levels
+        self.reached = st.reached
+        self.alg_bytes = st.alg_bytes
+        k = min(st.num_steps, st.max_steps)
+        self.steps = [dict(kind=STEP_NAME[steps[i].kind], level=steps[i].level,
+                           count=steps[i].count, edges=steps[i].edges,
+                           unvisited=steps[i].unvisited, seconds=steps[i].seconds)
+                      for i in range(k)]
+
+    @property
+    def trace(self):
+        """(kind, count) pairs as the reference's PrintStep lines carry them."""
+        return [(s["kind"], s["count"] if s["kind"] in ("td", "bu") else 0) for s in self.steps]
+
+
+def _stats_block(instrument, max_steps=4096):
+    steps = (Step * max_steps)()
+    st = Stats()
+    st.steps = ctypes.cast(steps, ctypes.POINTER(Step))
+    st.max_steps = max_steps
+    st.instrument = 1 if instrument else 0
+    return st, steps
+
+
+def DOBFS(g, source, alpha=15, beta=18, depth=False, stats=False, instrument=False,
+          parent_out=None, depth_out=None):
+    """One direction-optimizing BFS; returns parent (and depth, stats on request).
+
+    parent uses the reference's output encoding: parent[source] == source and
+    -1 for vertices the search did not reach.
+    """
+    parent = parent_out if parent_out is not None else np.empty(g.n, dtype=np.int32)
+    dep = None
+    if depth:
+        dep = depth_out if depth_out is not None else np.empty(g.n, dtype=np.int32)
+    st, steps = _stats_block(instrument) if (stats or instrument) else (None, None)
+    _check(lib().gbbfs_bfs(g.handle, int(source), int(alpha), int(beta), _p(parent), _p(dep),
+                           ctypes.byref(st) if st is not None else None), "bfs")
+    out = [parent]
+    if depth:
+        out.append(dep)
+    if st is not None:
+        out.append(SearchStats(st, steps))
+    return out[0] if len(out) == 1 else tuple(out)
+
+
+def bfs_device(g, source, alpha=15, beta=18, want_depth=False, stats=False, instrument=False):
+    """The search with results left in HBM; returns SearchStats or None."""
+    st, steps = _stats_block(instrument) if (stats or instrument) else (None, None)
+    _check(lib().gbbfs_bfs_device(g.handle, int(source), int(alpha), int(beta),
+                                  1 if want_depth else 0,
+                                  ctypes.byref(st) if st is not None else None), "bfs_device")
+    return SearchStats(st, steps) if st is not None else None
+
+
+def results(g, parent_out=None, depth_out=None):
+    _check(lib().gbbfs_results(g.handle, _p(parent_out), _p(depth_out)), "results")
+
+
+def write_bfs_output(path, parent):
+    p = np.ascontiguousarray(parent, dtype=np.int32)
+    _check(lib().gbbfs_append_bfs_output(os.fsencode(path), _p(p), len(p)), "append_bfs_output")

@@ -1,0 +1,172 @@
+/*
+ * gbbfs — direction-optimizing BFS on one GB300 GPU, behind a plain C ABI.
+ *
+ * This is the drop-in boundary for the BFS hot path of DMM-GAPBS.  The
+ * reference has no FFI layer: its boundary is the kernel functor
+ * `pvector<NodeID> DOBFS(const Graph&, NodeID source, ...)` that `main` hands
+ * to BenchmarkKernel (src/bfs.cc:142, :268, :273; src/benchmark.h:118-145),
+ * the graph that Builder::MakeGraph constructs (src/builder.h:314-338,
+ * gapbs-verify/builder.h:231-252), the SourcePicker sequence
+ * (src/benchmark.h:49-88) and the bfs_output.txt file that BFSVerifier writes
+ * (src/bfs.cc:213-235).  Each entry point below names the reference interface
+ * it replaces.
+ *
+ * Conventions: every call returns a gbbfs status (GBBFS_OK == 0).  No C++
+ * exception crosses this boundary.  A graph handle owns one CUDA stream and
+ * its per-search device state; calls on one handle must not run concurrently
+ * (one handle per host thread).  Host arrays stay owned by the caller.
+ * NodeID is int32_t and edge offsets int64_t, as in the reference
+ * (src/benchmark.h:31, src/graph.h SGOffset).
+ */
+#ifndef GBBFS_H_
+#define GBBFS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define GBBFS_OK 0
+#define GBBFS_ERR_ARG 1     /* bad argument (NULL handle, source out of range, ...) */
+#define GBBFS_ERR_NOMEM 2   /* not enough free HBM (checked before allocating)      */
+#define GBBFS_ERR_CUDA 3    /* a CUDA runtime call failed                            */
+#define GBBFS_ERR_TIMEOUT 4 /* a bounded device-side wait gave up                    */
+#define GBBFS_ERR_BOUNDS 5  /* a device-side bounds check fired                      */
+#define GBBFS_ERR_STATE 6   /* call out of order (e.g. results before a search)      */
+#define GBBFS_ERR_IO 7      /* file could not be read or written                     */
+
+/* Step kinds of the per-search trace, in the order the reference prints them
+ * with PrintStep (gapbs-verify/bfs.cc:124-165, src/bfs.cc:144-184). */
+#define GBBFS_STEP_TD 1 /* "td <next frontier size>"              */
+#define GBBFS_STEP_E 2  /* "e"  QueueToBitmap (top-down -> bottom-up) */
+#define GBBFS_STEP_BU 3 /* "bu <awake count>"                     */
+#define GBBFS_STEP_C 4  /* "c"  BitmapToQueue (bottom-up -> top-down) */
+
+typedef struct gbbfs_step {
+  int32_t kind;    /* GBBFS_STEP_*                                          */
+  int32_t level;   /* BFS depth the step discovers (0 for e/c)             */
+  int64_t count;   /* td: vertices claimed; bu: awake count; e/c: frontier */
+  int64_t edges;   /* td: edges examined; bu: in-neighbours scanned (instrumented) */
+  int64_t unvisited; /* bu: unvisited vertices at step start (instrumented) */
+  double seconds;  /* device time of the step (0 when not measured)        */
+} gbbfs_step;
+
+typedef struct gbbfs_stats {
+  /* in */
+  gbbfs_step* steps;   /* caller array for the trace, may be NULL            */
+  int32_t max_steps;   /* its capacity                                        */
+  int32_t instrument;  /* 1: count scanned edges and algorithmic bytes (slower) */
+  /* out */
+  int32_t num_steps;   /* records the search produced (may exceed max_steps) */
+  int32_t levels;      /* number of BFS levels discovered                   */
+  double device_ms;    /* device time of the whole search, init included     */
+  double init_seconds; /* device time of InitParent + frontier set-up ("i") */
+  int64_t reached;     /* vertices with a parent (source included)          */
+  int64_t alg_bytes;   /* algorithmic bytes of the search (instrument only) */
+} gbbfs_stats;
+
+typedef struct gbbfs_graph gbbfs_graph;
+
+/* Upload a CSR graph to HBM.  Replaces the Graph that
+ * Builder::MakeGraph returns (src/builder.h:314-338): offsets int64[n+1]
+ * (offsets[0] == 0, non-decreasing), neigh int32[m_dir] with
+ * m_dir == offsets[n].  The graph must be symmetric (undirected CSR, in-
+ * neighbours == out-neighbours, src/graph.h:280-290) as every synthetic graph
+ * of the reference is.  The caller keeps the host arrays. */
+int gbbfs_graph_create(const int64_t* offsets, const int32_t* neigh, int64_t n,
+                       int64_t m_dir, gbbfs_graph** out);
+
+/* Free the device copy (the graph's destructor, src/graph.h). */
+int gbbfs_graph_destroy(gbbfs_graph* g);
+
+/* n, m_dir and the bytes this handle holds on the device. */
+int gbbfs_graph_info(const gbbfs_graph* g, int64_t* n, int64_t* m_dir,
+                     int64_t* device_bytes);
+
+/* One direction-optimizing BFS from `source`: the kernel functor
+ * DOBFS(g, source, alpha, beta) (src/bfs.cc:142-188,
+ * gapbs-verify/bfs.cc:122-173).  alpha/beta <= 0 select the reference
+ * defaults 15 and 18.  parent_out (host, n entries, may be NULL) receives the
+ * BFS tree in the reference's output encoding: parent[source] == source,
+ * -1 for unreached vertices (src/bfs.cc:224-228).  depth_out (host, may be
+ * NULL) receives the BFS depth, -1 when unreached.  st (may be NULL) receives
+ * the step trace and timings. */
+int gbbfs_bfs(gbbfs_graph* g, int32_t source, int alpha, int beta,
+              int32_t* parent_out, int32_t* depth_out, gbbfs_stats* st);
+
+/* The same search with its results left in HBM (no device->host copy); read
+ * them with gbbfs_results.  want_depth != 0 also maintains the depth array. */
+int gbbfs_bfs_device(gbbfs_graph* g, int32_t source, int alpha, int beta,
+                     int want_depth, gbbfs_stats* st);
+
+/* Copy the results of the last search to the host (either may be NULL). */
+int gbbfs_results(gbbfs_graph* g, int32_t* parent_out, int32_t* depth_out);
+
+/* Device pointers of the last search's results (valid until the next call
+ * on the handle).  *depth is NULL if the search did not keep depths. */
+int gbbfs_result_device_ptrs(gbbfs_graph* g, const int32_t** parent,
+                             const int32_t** depth);
+
+/* Human-readable name of a status code. */
+const char* gbbfs_strerror(int status);
+
+/* Detail of the last failure on the calling thread ("" if none). */
+const char* gbbfs_last_error(void);
+
+/* ---- Host side of the path (C++ inside the library, no GPU needed) ---- */
+
+/* Build the symmetrized synthetic graph the reference builds for -g/-u
+ * <scale> -k <degree>: Generator::GenerateEL (gapbs-verify/generator.h:54-130,
+ * src/generator.h:66-167) then Builder::MakeGraphFromEL + SquishGraph
+ * (gapbs-verify/builder.h:191-252).  Bit-identical to the reference on the
+ * same libstdc++.  *offsets_out / *neigh_out are allocated with malloc; free
+ * them with gbbfs_free_host. */
+int gbbfs_generate(int scale, int degree, int uniform, int64_t** offsets_out,
+                   int32_t** neigh_out, int64_t* n_out, int64_t* m_dir_out);
+
+void gbbfs_free_host(void* p);
+
+/* The two halves of gbbfs_generate.  gbbfs_generate_edges returns the raw
+ * edge list (2 int32 per edge: u, v) of Generator::GenerateEL; gbbfs_build_csr
+ * turns any edge list into the symmetrized, squished CSR of
+ * Builder::MakeGraphFromEL + SquishGraph.  num_nodes < 0 means "largest id +
+ * 1" (gapbs-verify/builder.h:213-214). */
+int gbbfs_generate_edges(int scale, int degree, int uniform, int32_t** el_out,
+                         int64_t* edges_out);
+int gbbfs_build_csr(int32_t* el_pairs, int64_t edges, int64_t num_nodes,
+                    int64_t** offsets_out, int32_t** neigh_out, int64_t* n_out,
+                    int64_t* m_dir_out);
+
+/* Read a graph file the way Builder::MakeGraph does for -f
+ * (src/reader.h:57-257, :291-345): ".sg" serialized graphs (undirected only),
+ * ".el" / ".wel" edge lists ("u v [w]" per line, weights ignored) and DIMACS
+ * ".gr" ("a u v w" lines, 1-based ids).  Edge lists must be symmetrized
+ * (symmetrize != 0, the -s flag): this engine runs on undirected CSR only. */
+int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
+                     int32_t** neigh_out, int64_t* n_out, int64_t* m_dir_out);
+
+/* Write an undirected CSR as a ".sg" serialized graph (src/writer.h:39-69):
+ * bool directed, int64 num_edges_directed, int64 num_nodes, int64
+ * offsets[n+1], int32 neigh[m]. */
+int gbbfs_write_sg(const char* path, const int64_t* offsets, const int32_t* neigh,
+                   int64_t n, int64_t m_dir);
+
+/* SourcePicker::PickNext repeated `count` times (src/benchmark.h:49-88,
+ * gapbs-verify/benchmark.h:46-68): mt19937(27491095), uniform over [0, n-1],
+ * skipping out-degree-0 vertices; given != -1 (the -r flag) repeats it. */
+int gbbfs_pick_sources(const int64_t* offsets, int64_t n, int64_t given,
+                       int count, int32_t* out);
+
+/* Append one trial to a bfs_output.txt-format file: n lines, one decimal
+ * parent per line, -1 for every parent < 0 (BFSVerifier writer,
+ * src/bfs.cc:213-235). */
+int gbbfs_append_bfs_output(const char* path, const int32_t* parent, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBBFS_H_ */

@@ -1,0 +1,85 @@
+// Test-infrastructure driver around the reference's own shared-memory GAPBS BFS.
+//
+// It is compiled here, from the reference sources where they lie
+// (gapbs-verify/bfs.cc and the headers it includes), by oracle/build.py into
+// oracle/_ref/.  Nothing in the product links it.  It exists to pin the oracle
+// restatement (oracle/gapbs_oracle.cc) and to generate the golden fixtures
+// under tests/golden/.
+//
+// Usage:  gapbs_ref <mode> <out-prefix> <CLApp flags ...>
+//   graph   : write <prefix>.off (int64[n+1]) and <prefix>.nbr (int32[m]) of the
+//             graph Builder(cli).MakeGraph() builds (gapbs-verify/builder.h:231-252)
+//   sources : print -n SourcePicker picks, one per line (gapbs-verify/benchmark.h:46-68)
+//   bfs     : run DOBFS (gapbs-verify/bfs.cc:122-173) for -n trials, stdout carries the
+//             reference's own PrintStep trace; parents of all trials are appended
+//             to <prefix>.par (int32[n] per trial)
+//   time    : time DOBFS for -n trials (as src/benchmark.h:127-129 brackets it) and
+//             print one "trial <source> <seconds> <reached_degree_sum>" line each
+#define main gapbs_verify_bfs_main
+#include "bfs.cc"
+#undef main
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+
+static int64_t ReachedDegreeSum(const Graph &g, const pvector<NodeID> &parent) {
+  int64_t s = 0;
+  for (NodeID v = 0; v < g.num_nodes(); v++)
+    if (parent[v] >= 0) s += g.out_degree(v);
+  return s;
+}
+
+int main(int argc, char* argv[]) {
+  if (argc < 3) {
+    fprintf(stderr, "usage: %s graph|sources|bfs|time <out-prefix> <flags>\n", argv[0]);
+    return 2;
+  }
+  std::string mode = argv[1];
+  std::string prefix = argv[2];
+  argv[2] = argv[0];
+  CLApp cli(argc - 2, argv + 2, "breadth-first search (reference driver)");
+  if (!cli.ParseArgs())
+    return 3;
+  Builder b(cli);
+  Graph g = b.MakeGraph();
+  g.PrintStats();
+  if (mode == "graph") {
+    pvector<SGOffset> off = g.VertexOffsets(false);
+    std::ofstream fo(prefix + ".off", std::ios::binary);
+    fo.write(reinterpret_cast<const char*>(off.data()), sizeof(SGOffset) * (g.num_nodes() + 1));
+    std::ofstream fn(prefix + ".nbr", std::ios::binary);
+    for (NodeID u = 0; u < g.num_nodes(); u++)
+      for (NodeID v : g.out_neigh(u))
+        fn.write(reinterpret_cast<const char*>(&v), sizeof(NodeID));
+    return 0;
+  }
+  SourcePicker<Graph> sp(g, cli.start_vertex());
+  if (mode == "sources") {
+    for (int i = 0; i < cli.num_trials(); i++)
+      printf("%d\n", sp.PickNext());
+    return 0;
+  }
+  if (mode == "bfs") {
+    std::ofstream fp(prefix + ".par", std::ios::binary);
+    for (int i = 0; i < cli.num_trials(); i++) {
+      pvector<NodeID> parent = DOBFS(g, sp.PickNext());
+      fp.write(reinterpret_cast<const char*>(parent.data()), sizeof(NodeID) * g.num_nodes());
+    }
+    return 0;
+  }
+  if (mode == "time") {
+    for (int i = 0; i < cli.num_trials(); i++) {
+      NodeID s = sp.PickNext();
+      Timer t;
+      t.Start();
+      pvector<NodeID> parent = DOBFS(g, s);
+      t.Stop();
+      printf("trial %d %.9f %lld\n", s, t.Seconds(), (long long)ReachedDegreeSum(g, parent));
+    }
+    return 0;
+  }
+  fprintf(stderr, "unknown mode %s\n", mode.c_str());
+  return 2;
+}
