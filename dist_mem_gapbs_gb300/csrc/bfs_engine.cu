@@ -1,13 +1,23 @@
 // Host side of the GB300 BFS engine and its C ABI (include/gbbfs.h).
 //
-// gbbfs_graph holds the device CSR and the per-search state.  gbbfs_bfs runs
+// gbbfs_graph holds the device CSR and the per-search state.  A search runs
 // the DOBFS control loop of the reference (src/bfs.cc:142-188,
-// gapbs-verify/bfs.cc:122-173): the same alpha/beta tests on the same int64
-// counters, so the step sequence and its counts equal the reference's.
+// gapbs-verify/bfs.cc:122-173) on the device: k_decide applies the same
+// alpha/beta tests on the same int64 counters after every step, so the step
+// sequence and its counts equal the reference's.
+//
+// Two drivers share those kernels:
+//  * graph mode (default): one CUDA graph per handle —
+//      init -> while(loop) { decide -> switch(sel) { td | q2b | bu0 | bu1 | b2q } }
+//           -> copy of the state header back to pinned host memory
+//    so a whole search is one cudaGraphLaunch with no host round trip;
+//  * stepped mode: the host launches decide, reads the decision, launches the
+//    chosen kernel between two CUDA events.  It gives per-kernel event times.
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -33,6 +43,14 @@ thread_local std::string g_last_error;
     }                                                                         \
   } while (0)
 
+#define GB_TRY(x)            \
+  do {                       \
+    int st_ = (x);           \
+    if (st_ != GBBFS_OK) {   \
+      return st_;            \
+    }                        \
+  } while (0)
+
 int bit_length(uint64_t x) {
   int b = 0;
   while (x) {
@@ -41,6 +59,10 @@ int bit_length(uint64_t x) {
   }
   return b;
 }
+
+constexpr size_t kParamBytes = offsetof(DevState, edges_to_check);
+constexpr size_t kHeaderBytes = offsetof(DevState, trace);
+constexpr size_t kReadbackBytes = kHeaderBytes + kTraceInline * sizeof(DevStep);
 
 }  // namespace
 
@@ -60,10 +82,13 @@ struct gbbfs_graph {
   int32_t* qv[2] = {nullptr, nullptr};
   void* qs[2] = {nullptr, nullptr};
   DevCounters* ctr = nullptr;
-  DevCounters* h_ctr = nullptr;   // pinned mirror
+  DevState* st = nullptr;
+  DevState* h_st = nullptr;       // pinned mirror (params in, header + trace out)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
   std::vector<cudaEvent_t> step_ev;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
   int grid_init = 0, grid_td = 0, grid_bu = 0, grid_q2b = 0, grid_b2q = 0;
   int64_t device_bytes = 0;
   bool have_result = false;
@@ -75,6 +100,9 @@ namespace {
 void release(gbbfs_graph* g) {
   if (!g) return;
   if (g->device >= 0) cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->off);
   cudaFree(g->nbr);
   cudaFree(g->iso);
@@ -88,7 +116,8 @@ void release(gbbfs_graph* g) {
   cudaFree(g->qs[0]);
   cudaFree(g->qs[1]);
   cudaFree(g->ctr);
-  if (g->h_ctr) cudaFreeHost(g->h_ctr);
+  cudaFree(g->st);
+  if (g->h_st) cudaFreeHost(g->h_st);
   for (cudaEvent_t e : g->step_ev) cudaEventDestroy(e);
   if (g->ev_begin) cudaEventDestroy(g->ev_begin);
   if (g->ev_end) cudaEventDestroy(g->ev_end);
@@ -108,15 +137,30 @@ int dev_alloc(gbbfs_graph* g, T** p, size_t count) {
   return GBBFS_OK;
 }
 
-#define GB_TRY(x)            \
-  do {                       \
-    int st_ = (x);           \
-    if (st_ != GBBFS_OK) {   \
-      return st_;            \
-    }                        \
-  } while (0)
-
 template <typename OffT>
+Bufs<OffT> bufs(const gbbfs_graph* g) {
+  Bufs<OffT> b;
+  b.off = reinterpret_cast<const OffT*>(g->off);
+  b.nbr = g->nbr;
+  b.iso = g->iso;
+  b.visited = g->visited;
+  b.bm0 = g->bm[0];
+  b.bm1 = g->bm[1];
+  b.parent = g->parent;
+  b.depth = g->depth;
+  b.qv0 = g->qv[0];
+  b.qv1 = g->qv[1];
+  b.qs0 = reinterpret_cast<OffT*>(g->qs[0]);
+  b.qs1 = reinterpret_cast<OffT*>(g->qs[1]);
+  b.ctr = g->ctr;
+  b.st = g->st;
+  b.n = g->n;
+  b.m = g->m;
+  b.W = g->W;
+  b.shift = g->shift;
+  return b;
+}
+
 int occupancy_grid(const void* fn, int sms, int* grid) {
   int per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
@@ -126,11 +170,11 @@ int occupancy_grid(const void* fn, int sms, int* grid) {
 
 template <typename OffT>
 int setup_grids(gbbfs_graph* g) {
-  GB_TRY(occupancy_grid<OffT>((const void*)k_init<OffT>, g->sms, &g->grid_init));
-  GB_TRY(occupancy_grid<OffT>((const void*)k_td<OffT>, g->sms, &g->grid_td));
-  GB_TRY(occupancy_grid<OffT>((const void*)k_bu<OffT, false>, g->sms, &g->grid_bu));
-  GB_TRY(occupancy_grid<OffT>((const void*)k_q2b, g->sms, &g->grid_q2b));
-  GB_TRY(occupancy_grid<OffT>((const void*)k_b2q<OffT>, g->sms, &g->grid_b2q));
+  GB_TRY(occupancy_grid((const void*)k_init<OffT>, g->sms, &g->grid_init));
+  GB_TRY(occupancy_grid((const void*)k_td<OffT>, g->sms, &g->grid_td));
+  GB_TRY(occupancy_grid((const void*)k_bu<OffT, 0>, g->sms, &g->grid_bu));
+  GB_TRY(occupancy_grid((const void*)k_q2b<OffT>, g->sms, &g->grid_q2b));
+  GB_TRY(occupancy_grid((const void*)k_b2q<OffT>, g->sms, &g->grid_b2q));
   return GBBFS_OK;
 }
 
@@ -183,7 +227,7 @@ int create(const int64_t* offsets, const int32_t* neigh, int64_t n, int64_t m,
   // Admission: everything this handle allocates, against free HBM.
   const size_t need = offsz * (n + 1) + 4 * (size_t)m + 4 * 4 * (size_t)g->W +
                       2 * 4 * 32 * (size_t)g->W + 2 * (4 + offsz) * (size_t)(n + 1) +
-                      8 * (n + 1) + (64 << 20);
+                      8 * (n + 1) + sizeof(DevState) + (64 << 20);
   size_t free_b = 0, total_b = 0;
   GB_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (need > free_b) {
@@ -215,161 +259,165 @@ int create(const int64_t* offsets, const int32_t* neigh, int64_t n, int64_t m,
     }
   }
   GB_TRY(dev_alloc(g, &g->ctr, 1));
-  GB_CUDA(cudaHostAlloc(&g->h_ctr, sizeof(DevCounters), cudaHostAllocDefault));
+  GB_TRY(dev_alloc(g, &g->st, 1));
+  GB_CUDA(cudaHostAlloc(&g->h_st, sizeof(DevState), cudaHostAllocDefault));
+  memset(g->h_st, 0, sizeof(DevState));
   GB_CUDA(cudaMemsetAsync(g->ctr, 0, sizeof(DevCounters), g->stream));
+  GB_CUDA(cudaMemsetAsync(g->st, 0, sizeof(DevState), g->stream));
   if (g->off32) return upload<uint32_t>(g, offsets, neigh);
   return upload<unsigned long long>(g, offsets, neigh);
 }
 
-// Copy the counters to the pinned mirror and wait for them.
-int read_counters(gbbfs_graph* g) {
-  GB_CUDA(cudaMemcpyAsync(g->h_ctr, g->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost,
-                          g->stream));
-  GB_CUDA(cudaStreamSynchronize(g->stream));
+// ---------------------------------------------------------------------------
+// Graph mode.
+
+int add_kernel(cudaGraphNode_t* node, cudaGraph_t graph, const cudaGraphNode_t* deps,
+               size_t ndeps, const void* fn, int grid, int block, void** args) {
+  cudaKernelNodeParams kp;
+  memset(&kp, 0, sizeof kp);
+  kp.func = const_cast<void*>(fn);
+  kp.gridDim = dim3(grid);
+  kp.blockDim = dim3(block);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  GB_CUDA(cudaGraphAddKernelNode(node, graph, deps, ndeps, &kp));
   return GBBFS_OK;
 }
 
-struct StepLog {
-  std::vector<gbbfs_step> steps;
-  bool timed = false;
-  double init_seconds = 0;
-};
-
-// The DOBFS control loop with one host round trip per step.
 template <typename OffT>
-int run_search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
-               bool instrument, StepLog* log, int* levels_out, int64_t* reached_out) {
-  const OffT* off = reinterpret_cast<const OffT*>(g->off);
-  OffT* qs[2] = {reinterpret_cast<OffT*>(g->qs[0]), reinterpret_cast<OffT*>(g->qs[1])};
-  int32_t* depth = want_depth ? g->depth : nullptr;
-  cudaStream_t s = g->stream;
-  const int shift = g->shift;
-  const unsigned long long emask = (1ull << shift) - 1;
-  uint32_t* front = g->bm[0];
-  uint32_t* next = g->bm[1];
-  int cur = 0;
+int build_graph(gbbfs_graph* g) {
+  Bufs<OffT> b = bufs<OffT>(g);
+  cudaGraph_t graph;
+  GB_CUDA(cudaGraphCreate(&graph, 0));
+  g->graph = graph;
+  cudaGraphConditionalHandle h_loop;
+  GB_CUDA(cudaGraphConditionalHandleCreate(&h_loop, graph, 1, cudaGraphCondAssignDefault));
+  void* args_b[] = {&b};
+  cudaGraphNode_t init_node;
+  GB_TRY(add_kernel(&init_node, graph, nullptr, 0, (const void*)k_init<OffT>, g->grid_init,
+                    kThreads, args_b));
+  cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+  wp.conditional.handle = h_loop;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t loop_node;
+  GB_CUDA(cudaGraphAddNode(&loop_node, graph, &init_node, nullptr, 1, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
 
-  auto mark = [&](size_t idx) -> int {
-    if (!log->timed) return GBBFS_OK;
-    while (g->step_ev.size() <= idx) {
-      cudaEvent_t e;
-      GB_CUDA(cudaEventCreate(&e));
-      g->step_ev.push_back(e);
-    }
-    GB_CUDA(cudaEventRecord(g->step_ev[idx], s));
-    return GBBFS_OK;
-  };
-  auto push = [&](int kind, int level, int64_t count, int64_t edges, int64_t unvisited) {
-    gbbfs_step st;
-    st.kind = kind;
-    st.level = level;
-    st.count = count;
-    st.edges = edges;
-    st.unvisited = unvisited;
-    st.seconds = 0;
-    log->steps.push_back(st);
-  };
+  cudaGraphConditionalHandle h_sel;
+  GB_CUDA(cudaGraphConditionalHandleCreate(&h_sel, body, kSelNone, cudaGraphCondAssignDefault));
+  void* args_d[] = {&b, &h_loop, &h_sel};
+  cudaGraphNode_t decide_node;
+  GB_TRY(add_kernel(&decide_node, body, nullptr, 0, (const void*)k_decide<OffT>, 1, 32,
+                    args_d));
+  cudaGraphNodeParams sp = {cudaGraphNodeTypeConditional};
+  sp.conditional.handle = h_sel;
+  sp.conditional.type = cudaGraphCondTypeSwitch;
+  sp.conditional.size = 5;
+  cudaGraphNode_t switch_node;
+  GB_CUDA(cudaGraphAddNode(&switch_node, body, &decide_node, nullptr, 1, &sp));
+  cudaGraphNode_t k;
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelTD], nullptr, 0,
+                    (const void*)k_td<OffT>, g->grid_td, kThreads, args_b));
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelQ2B], nullptr, 0,
+                    (const void*)k_q2b<OffT>, g->grid_q2b, kThreads, args_b));
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelBU0], nullptr, 0,
+                    (const void*)k_bu<OffT, 0>, g->grid_bu, kThreads, args_b));
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelBU1], nullptr, 0,
+                    (const void*)k_bu<OffT, 1>, g->grid_bu, kThreads, args_b));
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelB2Q], nullptr, 0,
+                    (const void*)k_b2q<OffT>, g->grid_b2q, kThreads, args_b));
 
-  GB_CUDA(cudaEventRecord(g->ev_begin, s));
-  k_init<OffT><<<g->grid_init, kThreads, 0, s>>>(g->n, g->W, off, g->iso, g->visited, front,
-                                                g->parent, depth, source, g->qv[0], qs[0],
-                                                g->ctr, shift);
-  GB_CUDA(cudaGetLastError());
-  GB_TRY(mark(0));  // end of "i"
-  GB_TRY(read_counters(g));
-  int64_t F = (int64_t)(g->h_ctr->qpacked[0] >> shift);
-  int64_t scout = (int64_t)(g->h_ctr->qpacked[0] & emask);
-  int64_t cur_edges = scout;  // summed degrees of the current queue
-  int64_t edges_to_check = g->m;
-  int64_t visited = 1;
-  int level = 1;
-  while (F > 0) {
-    if (scout > edges_to_check / alpha) {
-      // QueueToBitmap ("e")
-      GB_TRY(mark(1 + 2 * log->steps.size()));
-      k_q2b<<<g->grid_q2b, kThreads, 0, s>>>(g->qv[cur], g->ctr, cur, shift, front);
-      GB_CUDA(cudaGetLastError());
-      GB_TRY(mark(2 + 2 * log->steps.size()));
-      push(GBBFS_STEP_E, 0, F, 0, 0);
-      int64_t awake = F, old_awake;
-      do {
-        old_awake = awake;
-        GB_TRY(mark(1 + 2 * log->steps.size()));
-        GB_CUDA(cudaMemsetAsync(&g->ctr->awake, 0, 2 * sizeof(unsigned long long), s));
-        if (instrument)
-          k_bu<OffT, true><<<g->grid_bu, kThreads, 0, s>>>(g->W, off, g->nbr, g->visited,
-                                                          g->parent, depth, front, next,
-                                                          g->ctr, level);
-        else
-          k_bu<OffT, false><<<g->grid_bu, kThreads, 0, s>>>(g->W, off, g->nbr, g->visited,
-                                                           g->parent, depth, front, next,
-                                                           g->ctr, level);
-        GB_CUDA(cudaGetLastError());
-        GB_TRY(mark(2 + 2 * log->steps.size()));
-        GB_TRY(read_counters(g));
-        awake = (int64_t)g->h_ctr->awake;
-        push(GBBFS_STEP_BU, level, awake, instrument ? (int64_t)g->h_ctr->scanned : 0,
-             g->n - visited);
-        visited += awake;
-        std::swap(front, next);
-        level++;
-      } while (awake >= old_awake || awake > g->n / beta);
-      // BitmapToQueue ("c")
-      GB_TRY(mark(1 + 2 * log->steps.size()));
-      GB_CUDA(cudaMemsetAsync(&g->ctr->qpacked[cur], 0, sizeof(unsigned long long), s));
-      k_b2q<OffT><<<g->grid_b2q, kThreads, 0, s>>>(g->W, off, front, g->qv[cur], qs[cur],
-                                                    g->ctr, cur, shift);
-      GB_CUDA(cudaGetLastError());
-      GB_TRY(mark(2 + 2 * log->steps.size()));
-      GB_TRY(read_counters(g));
-      F = (int64_t)(g->h_ctr->qpacked[cur] >> shift);
-      cur_edges = (int64_t)(g->h_ctr->qpacked[cur] & emask);
-      push(GBBFS_STEP_C, 0, F, 0, 0);
-      scout = 1;
-    } else {
-      edges_to_check -= scout;
-      const int nxt = cur ^ 1;
-      GB_TRY(mark(1 + 2 * log->steps.size()));
-      GB_CUDA(cudaMemsetAsync(&g->ctr->qpacked[nxt], 0, sizeof(unsigned long long), s));
-      k_td<OffT><<<g->grid_td, kThreads, 0, s>>>(off, g->nbr, g->visited, g->parent, depth,
-                                                  g->qv[cur], qs[cur], g->qv[nxt], qs[nxt],
-                                                  g->ctr, cur, shift, level);
-      GB_CUDA(cudaGetLastError());
-      GB_TRY(mark(2 + 2 * log->steps.size()));
-      GB_TRY(read_counters(g));
-      F = (int64_t)(g->h_ctr->qpacked[nxt] >> shift);
-      scout = (int64_t)(g->h_ctr->qpacked[nxt] & emask);
-      push(GBBFS_STEP_TD, level, F, cur_edges, 0);
-      cur_edges = scout;
-      visited += F;
-      cur = nxt;
-      level++;
-    }
+  cudaGraphNode_t copy_node;
+  GB_CUDA(cudaGraphAddMemcpyNode1D(&copy_node, graph, &loop_node, 1, g->h_st, g->st,
+                                   kReadbackBytes, cudaMemcpyDeviceToHost));
+  GB_CUDA(cudaGraphInstantiate(&g->exec, graph, 0));
+  return GBBFS_OK;
+}
+
+template <typename OffT>
+int run_graph(gbbfs_graph* g) {
+  if (!g->exec) GB_TRY(build_graph<OffT>(g));
+  GB_CUDA(cudaMemcpyAsync(g->st, g->h_st, kParamBytes, cudaMemcpyHostToDevice, g->stream));
+  GB_CUDA(cudaEventRecord(g->ev_begin, g->stream));
+  GB_CUDA(cudaGraphLaunch(g->exec, g->stream));
+  GB_CUDA(cudaEventRecord(g->ev_end, g->stream));
+  GB_CUDA(cudaEventSynchronize(g->ev_end));
+  return GBBFS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stepped mode: same kernels, decisions read back after every k_decide.
+
+int step_event(gbbfs_graph* g, size_t idx) {
+  while (g->step_ev.size() <= idx) {
+    cudaEvent_t e;
+    GB_CUDA(cudaEventCreate(&e));
+    g->step_ev.push_back(e);
   }
+  GB_CUDA(cudaEventRecord(g->step_ev[idx], g->stream));
+  return GBBFS_OK;
+}
+
+template <typename OffT>
+int run_stepped(gbbfs_graph* g, std::vector<double>* kernel_seconds) {
+  Bufs<OffT> b = bufs<OffT>(g);
+  cudaStream_t s = g->stream;
+  GB_CUDA(cudaMemcpyAsync(g->st, g->h_st, kParamBytes, cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaEventRecord(g->ev_begin, s));
+  k_init<OffT><<<g->grid_init, kThreads, 0, s>>>(b);
+  GB_CUDA(cudaGetLastError());
+  const size_t ctl = offsetof(DevState, cur);
+  size_t steps = 0;
+  for (;;) {
+    k_decide<OffT><<<1, 32, 0, s>>>(b, 0, 0);
+    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(g->h_st) + ctl,
+                            reinterpret_cast<char*>(g->st) + ctl, 4 * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    const int kind = g->h_st->next_kind;
+    if (kind == kKindStop) break;
+    GB_TRY(step_event(g, 2 * steps));
+    switch (kind) {
+      case kKindTD: k_td<OffT><<<g->grid_td, kThreads, 0, s>>>(b); break;
+      case kKindE: k_q2b<OffT><<<g->grid_q2b, kThreads, 0, s>>>(b); break;
+      case kKindBU:
+        if (g->h_st->parity)
+          k_bu<OffT, 1><<<g->grid_bu, kThreads, 0, s>>>(b);
+        else
+          k_bu<OffT, 0><<<g->grid_bu, kThreads, 0, s>>>(b);
+        break;
+      case kKindC: k_b2q<OffT><<<g->grid_b2q, kThreads, 0, s>>>(b); break;
+      default:
+        g_last_error = "unknown step kind from the device";
+        return GBBFS_ERR_STATE;
+    }
+    GB_CUDA(cudaGetLastError());
+    GB_TRY(step_event(g, 2 * steps + 1));
+    steps++;
+  }
+  GB_CUDA(cudaMemcpyAsync(g->h_st, g->st, kReadbackBytes, cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaEventRecord(g->ev_end, s));
   GB_CUDA(cudaEventSynchronize(g->ev_end));
-  if (log->timed) {
-    float init_ms = 0;
-    GB_CUDA(cudaEventElapsedTime(&init_ms, g->ev_begin, g->step_ev[0]));
-    log->init_seconds = init_ms * 1e-3;
-    for (size_t i = 0; i < log->steps.size(); i++) {
-      float ms = 0;
-      GB_CUDA(cudaEventElapsedTime(&ms, g->step_ev[1 + 2 * i], g->step_ev[2 + 2 * i]));
-      log->steps[i].seconds = ms * 1e-3;
-    }
+  kernel_seconds->resize(steps);
+  for (size_t i = 0; i < steps; i++) {
+    float ms = 0;
+    GB_CUDA(cudaEventElapsedTime(&ms, g->step_ev[2 * i], g->step_ev[2 * i + 1]));
+    (*kernel_seconds)[i] = ms * 1e-3;
   }
-  *levels_out = level;
-  *reached_out = visited;
   return GBBFS_OK;
 }
 
-int64_t alg_bytes(int64_t n, const std::vector<gbbfs_step>& steps) {
+int64_t alg_bytes(int64_t n, const gbbfs_step* steps, int count) {
   // InitParent 12n; TD 20|F| + 8 E_td + 8|N|; BU 4n + n/4 + 8|U| + 4 E_bu + 4|N|;
   // TD->BU 4|F| + n/8; BU->TD n/8 + 4|F'|.  |F| of a td step is the count of
   // the step before it.
   int64_t b = 12 * n;
   int64_t prev = 1;
-  for (const gbbfs_step& s : steps) {
+  for (int i = 0; i < count; i++) {
+    const gbbfs_step& s = steps[i];
     switch (s.kind) {
       case GBBFS_STEP_TD: b += 20 * prev + 8 * s.edges + 8 * s.count; break;
       case GBBFS_STEP_BU: b += 4 * n + n / 4 + 8 * s.unvisited + 4 * s.edges + 4 * s.count; break;
@@ -392,31 +440,57 @@ int search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
   if (beta <= 0) beta = 18;
   GB_CUDA(cudaSetDevice(g->device));
   g->have_result = false;
-  StepLog log;
-  log.timed = st && st->steps && st->max_steps > 0;
   const bool instrument = st && st->instrument;
-  int levels = 0;
-  int64_t reached = 0;
-  int rc = g->off32
-               ? run_search<uint32_t>(g, source, alpha, beta, want_depth, instrument, &log,
-                                      &levels, &reached)
-               : run_search<unsigned long long>(g, source, alpha, beta, want_depth,
-                                                instrument, &log, &levels, &reached);
+  const bool stepped = st && st->stepped;
+  DevState* h = g->h_st;
+  h->source = source;
+  h->alpha = alpha;
+  h->beta = beta;
+  h->want_depth = want_depth ? 1 : 0;
+  h->instrument = instrument ? 1 : 0;
+  h->in_graph = stepped ? 0 : 1;
+  std::vector<double> kernel_seconds;
+  int rc;
+  if (stepped)
+    rc = g->off32 ? run_stepped<uint32_t>(g, &kernel_seconds)
+                  : run_stepped<unsigned long long>(g, &kernel_seconds);
+  else
+    rc = g->off32 ? run_graph<uint32_t>(g) : run_graph<unsigned long long>(g);
   if (rc != GBBFS_OK) return rc;
+  if (h->error) {
+    g_last_error = "device control loop exceeded its iteration bound";
+    return h->error;
+  }
   g->have_result = true;
   g->result_depth = want_depth;
   if (st) {
     float ms = 0;
     GB_CUDA(cudaEventElapsedTime(&ms, g->ev_begin, g->ev_end));
     st->device_ms = ms;
-    st->init_seconds = log.init_seconds;
-    st->num_steps = (int32_t)log.steps.size();
-    st->levels = levels;
-    st->reached = reached;
-    st->alg_bytes = instrument ? alg_bytes(g->n, log.steps) : 0;
+    st->init_seconds = h->init_ns * 1e-9;
+    st->num_steps = h->nsteps;
+    st->levels = h->level - 1;
+    st->reached = h->visited;
+    const int have = std::min(h->nsteps, kMaxTrace);
+    std::vector<DevStep> tr(have);
+    if (have > 0) memcpy(tr.data(), h->trace, sizeof(DevStep) * std::min(have, kTraceInline));
+    if (have > kTraceInline) {
+      GB_CUDA(cudaMemcpy(tr.data() + kTraceInline, g->st->trace + kTraceInline,
+                         sizeof(DevStep) * (have - kTraceInline), cudaMemcpyDeviceToHost));
+    }
+    std::vector<gbbfs_step> steps(have);
+    for (int i = 0; i < have; i++) {
+      steps[i].kind = tr[i].kind;
+      steps[i].level = tr[i].level;
+      steps[i].count = tr[i].count;
+      steps[i].edges = tr[i].edges;
+      steps[i].unvisited = tr[i].unvisited;
+      steps[i].seconds = stepped && i < (int)kernel_seconds.size() ? kernel_seconds[i]
+                                                                   : tr[i].ns * 1e-9;
+    }
+    st->alg_bytes = instrument ? alg_bytes(g->n, steps.data(), have) : 0;
     if (st->steps)
-      for (int i = 0; i < st->max_steps && i < (int)log.steps.size(); i++)
-        st->steps[i] = log.steps[i];
+      for (int i = 0; i < st->max_steps && i < have; i++) st->steps[i] = steps[i];
   }
   return GBBFS_OK;
 }

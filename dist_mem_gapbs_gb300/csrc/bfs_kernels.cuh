@@ -5,16 +5,20 @@
 //   nbr      int32[m]    sorted neighbour lists (in == out: the graph is symmetric)
 //   iso      u32[W]      bit set for degree-0 vertices and ids >= n
 //   visited  u32[W]      bit set once a vertex has a parent
-//   front    u32[W]      bottom-up frontier; next u32[W] the one being built
+//   bm0/bm1  u32[W]      bottom-up frontier and the one being built (swap by parity)
 //   parent   int32[32W]  the BFS tree, -1 while unvisited
-//   depth    int32[32W]  BFS depth, -1 while unvisited (optional)
-//   qv/qs    frontier queue: vertex ids and the exclusive prefix sum of their
+//   depth    int32[32W]  BFS depth, -1 while unvisited (kept on request)
+//   qv/qs    frontier queues: vertex ids and the exclusive prefix sum of their
 //            out-degrees, in queue order (two of each, current and next)
 //
 // A bitmap word w covers vertices [32w, 32w+32); in bottom-up steps one warp
 // owns a word at a time, so next/visited/parent of that range have exactly
 // one writer and need no atomics (the reference's per-PE vertex ranges of
 // src/partition.h:69-161, one level finer).
+//
+// Every step kernel reads what changes from step to step (queue index,
+// frontier parity, level) from DevState, which k_decide writes, so the same
+// kernel nodes serve every level of a CUDA graph.
 #pragma once
 
 #include "bfs_common.cuh"
@@ -24,21 +28,20 @@ namespace gbbfs {
 // ---------------------------------------------------------------------------
 // InitParent (src/bfs.cc:131-140, gapbs-verify/bfs.cc:114-120) fused with the
 // frontier set-up of DOBFS (src/bfs.cc:150-159): parent = -1 everywhere, the
-// source its own parent, visited = iso | {source}, front = 0, queue = {source}.
+// source its own parent, visited = iso | {source}, bm0 = 0, queue = {source}.
 // The reference keeps -out_degree in parent for unvisited vertices so that
 // scout_count can sum it; here the degree is read from the offsets at claim
 // time instead, which keeps the init a pure store stream.
 template <typename OffT>
-__global__ void __launch_bounds__(kThreads)
-k_init(int64_t n, int64_t W, const OffT* __restrict__ off, const uint32_t* __restrict__ iso,
-       uint32_t* __restrict__ visited, uint32_t* __restrict__ front,
-       int32_t* __restrict__ parent, int32_t* __restrict__ depth, int32_t source,
-       int32_t* __restrict__ qv0, OffT* __restrict__ qs0, DevCounters* __restrict__ ctr,
-       int shift) {
+__global__ void __launch_bounds__(kThreads) k_init(Bufs<OffT> b) {
+  DevState* st = b.st;
+  stamp_begin(st);
+  const int32_t source = st->source;
+  int32_t* depth = st->want_depth ? b.depth : nullptr;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // parent / depth: 8 int32 per thread-iteration (32-byte stores).
-  const int64_t nvec = W * 4;  // 32W ints / 8
+  // parent / depth: 8 int32 per thread-iteration (two 16-byte stores).
+  const int64_t nvec = b.W * 4;
   const int64_t src_vec = source >> 3;
   const int src_lane = source & 7;
   auto put = [](int4 v, int lane, int val) {
@@ -52,28 +55,161 @@ k_init(int64_t n, int64_t W, const OffT* __restrict__ off, const uint32_t* __res
   for (int64_t i = tid; i < nvec; i += stride) {
     const bool here = i == src_vec;
     const int la = here ? src_lane : -1, lb = here ? src_lane - 4 : -1;
-    reinterpret_cast<int4*>(parent)[2 * i] = put(neg, la, source);
-    reinterpret_cast<int4*>(parent)[2 * i + 1] = put(neg, lb, source);
+    reinterpret_cast<int4*>(b.parent)[2 * i] = put(neg, la, source);
+    reinterpret_cast<int4*>(b.parent)[2 * i + 1] = put(neg, lb, source);
     if (depth) {
       reinterpret_cast<int4*>(depth)[2 * i] = put(neg, la, 0);
       reinterpret_cast<int4*>(depth)[2 * i + 1] = put(neg, lb, 0);
     }
   }
   const int64_t src_word = source >> 5;
-  for (int64_t w = tid; w < W; w += stride) {
-    uint32_t v = iso[w];
+  for (int64_t w = tid; w < b.W; w += stride) {
+    uint32_t v = b.iso[w];
     if (w == src_word) v |= 1u << (source & 31);
-    visited[w] = v;
-    front[w] = 0;
+    b.visited[w] = v;
+    b.bm0[w] = 0;
   }
   if (tid == 0) {
-    qv0[0] = source;
-    qs0[0] = 0;
-    const unsigned long long deg = (unsigned long long)(off[source + 1] - off[source]);
-    ctr->qpacked[0] = (1ull << shift) | deg;
-    ctr->qpacked[1] = 0;
-    ctr->awake = 0;
-    ctr->scanned = 0;
+    b.qv0[0] = source;
+    b.qs0[0] = 0;
+    const unsigned long long deg = (unsigned long long)(b.off[source + 1] - b.off[source]);
+    b.ctr->qpacked[0] = (1ull << b.shift) | deg;
+    b.ctr->qpacked[1] = 0;
+    b.ctr->awake = 0;
+    b.ctr->scanned = 0;
+    st->cur = 0;
+    st->parity = 0;
+    st->level = 1;
+    st->visited = 1;
+    st->edges_to_check = b.m;
+    st->iter = 0;
+    st->max_iter = 4 * b.n + 64;
+    st->nsteps = 0;
+    st->error = 0;
+    st->next_kind = kKindInit;
+  }
+  stamp_end(st);
+}
+
+// ---------------------------------------------------------------------------
+// The DOBFS control loop (src/bfs.cc:158-185, gapbs-verify/bfs.cc:138-166),
+// one decision per launch, on one thread.  It books the step that just ran
+// (trace record, counters), then applies the reference's tests on the same
+// int64 values:
+//   scout_count > edges_to_check / alpha          -> switch to bottom-up
+//   awake >= old_awake || awake > num_nodes / beta -> stay bottom-up
+// and selects the next step.  Inside a CUDA graph it steers the per-step
+// switch node and ends the while loop; stepped from the host it only writes
+// st->next_kind.  A bound on the iteration count (4 * num_nodes + 64: a
+// top-down or bottom-up step continues the loop only after claiming a vertex,
+// and at most two conversions sit between two such steps) stops a run-away
+// loop with GBBFS_ERR_TIMEOUT instead of spinning.
+template <typename OffT>
+__global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
+                         cudaGraphConditionalHandle h_sel) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  DevState* s = b.st;
+  DevCounters* c = b.ctr;
+  const unsigned long long emask = (1ull << b.shift) - 1;
+  const int64_t ns = s->t1 > s->t0 ? (int64_t)(s->t1 - s->t0) : 0;
+  auto rec = [&](int32_t kind, int32_t level, int64_t count, int64_t edges, int64_t unv) {
+    if (s->nsteps < kMaxTrace) {
+      DevStep& r = s->trace[s->nsteps];
+      r.kind = kind;
+      r.level = level;
+      r.count = count;
+      r.edges = edges;
+      r.unvisited = unv;
+      r.ns = ns;
+    }
+    s->nsteps++;
+  };
+  int32_t next = kKindStop;
+  bool frontier_decision = false;
+  switch (s->next_kind) {
+    case kKindInit: {
+      s->init_ns = ns;
+      const unsigned long long p = c->qpacked[0];
+      s->F = (int64_t)(p >> b.shift);
+      s->scout = (int64_t)(p & emask);
+      s->cur_edges = s->scout;
+      frontier_decision = true;
+      break;
+    }
+    case kKindTD: {
+      const int nxt = s->cur ^ 1;
+      const unsigned long long p = c->qpacked[nxt];
+      s->F = (int64_t)(p >> b.shift);
+      rec(kKindTD, s->level, s->F, s->cur_edges, 0);
+      s->scout = (int64_t)(p & emask);
+      s->cur_edges = s->scout;
+      s->visited += s->F;
+      s->cur = nxt;
+      s->level++;
+      frontier_decision = true;
+      break;
+    }
+    case kKindE:
+      rec(kKindE, 0, s->F, 0, 0);
+      s->awake = s->F;
+      next = kKindBU;
+      break;
+    case kKindBU: {
+      const int64_t awake = (int64_t)c->awake;
+      rec(kKindBU, s->level, awake, (int64_t)c->scanned, b.n - s->visited);
+      s->awake = awake;
+      s->visited += awake;
+      s->parity ^= 1;
+      s->level++;
+      next = (awake >= s->old_awake || awake > b.n / s->beta) ? kKindBU : kKindC;
+      break;
+    }
+    case kKindC: {
+      const unsigned long long p = c->qpacked[s->cur];
+      s->F = (int64_t)(p >> b.shift);
+      s->cur_edges = (int64_t)(p & emask);
+      rec(kKindC, 0, s->F, 0, 0);
+      s->scout = 1;
+      frontier_decision = true;
+      break;
+    }
+    default:
+      next = kKindStop;
+  }
+  if (frontier_decision) {
+    if (s->F == 0) {
+      next = kKindStop;
+    } else if (s->scout > s->edges_to_check / s->alpha) {
+      next = kKindE;
+    } else {
+      s->edges_to_check -= s->scout;
+      next = kKindTD;
+    }
+  }
+  if (++s->iter > s->max_iter && next != kKindStop) {
+    s->error = GBBFS_ERR_TIMEOUT;
+    next = kKindStop;
+  }
+  if (next == kKindBU) {
+    s->old_awake = s->awake;
+    c->awake = 0;
+    c->scanned = 0;
+  } else if (next == kKindTD) {
+    c->qpacked[s->cur ^ 1] = 0;
+  } else if (next == kKindC) {
+    c->qpacked[s->cur] = 0;
+  }
+  s->next_kind = next;
+  s->t0 = ~0ull;
+  s->t1 = 0;
+  if (s->in_graph) {
+    unsigned sel = kSelNone;
+    if (next == kKindTD) sel = kSelTD;
+    else if (next == kKindE) sel = kSelQ2B;
+    else if (next == kKindBU) sel = s->parity ? kSelBU1 : kSelBU0;
+    else if (next == kKindC) sel = kSelB2Q;
+    cudaGraphSetConditional(h_sel, sel);
+    cudaGraphSetConditional(h_loop, next != kKindStop ? 1u : 0u);
   }
 }
 
@@ -95,17 +231,25 @@ k_init(int64_t n, int64_t W, const OffT* __restrict__ off, const uint32_t* __res
 constexpr int kTdStage = 256;
 
 template <typename OffT>
-__global__ void __launch_bounds__(kThreads)
-k_td(const OffT* __restrict__ off, const int32_t* __restrict__ nbr, uint32_t* visited,
-     int32_t* __restrict__ parent, int32_t* __restrict__ depth,
-     const int32_t* __restrict__ qv, const OffT* __restrict__ qs,
-     int32_t* __restrict__ qv_out, OffT* __restrict__ qs_out,
-     DevCounters* __restrict__ ctr, int cur, int shift, int level) {
+__global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
   __shared__ int32_t st_v[kWarpsPerCta][kTdStage];
   __shared__ OffT st_d[kWarpsPerCta][kTdStage];
+  DevState* st = b.st;
+  stamp_begin(st);
+  const int cur = st->cur;
+  const int level = st->level;
+  int32_t* depth = st->want_depth ? b.depth : nullptr;
+  const int32_t* qv = cur ? b.qv1 : b.qv0;
+  const OffT* qs = cur ? b.qs1 : b.qs0;
+  int32_t* qv_out = cur ? b.qv0 : b.qv1;
+  OffT* qs_out = cur ? b.qs0 : b.qs1;
+  const OffT* __restrict__ off = b.off;
+  const int32_t* __restrict__ nbr = b.nbr;
+  uint32_t* visited = b.visited;
+  const int shift = b.shift;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const unsigned long long packed = ctr->qpacked[cur];
+  const unsigned long long packed = b.ctr->qpacked[cur];
   const int64_t F = (int64_t)(packed >> shift);
   const unsigned long long emask = (1ull << shift) - 1;
   const uint64_t E = packed & emask;
@@ -125,7 +269,7 @@ k_td(const OffT* __restrict__ off, const int32_t* __restrict__ nbr, uint32_t* vi
     for (int o = 16; o; o >>= 1) red += shfl(red, lane ^ o);
     unsigned long long base = 0;
     if (lane == 0)
-      base = atomicAdd(&ctr->qpacked[cur ^ 1],
+      base = atomicAdd(&b.ctr->qpacked[cur ^ 1],
                        ((unsigned long long)staged << shift) + (unsigned long long)red);
     base = shfl(base, 0);
     const uint64_t qbase = base >> shift;
@@ -184,7 +328,7 @@ k_td(const OffT* __restrict__ off, const int32_t* __restrict__ nbr, uint32_t* vi
           const uint32_t old = atomicOr(wp, bit);
           if (!(old & bit)) {
             claimed = true;
-            parent[v] = u;
+            b.parent[v] = u;
             if (depth) depth[v] = level;
             dv = __ldg(off + v + 1) - __ldg(off + v);
           }
@@ -212,20 +356,27 @@ k_td(const OffT* __restrict__ off, const int32_t* __restrict__ nbr, uint32_t* vi
     }
   }
   if (staged) flush();
+  stamp_end(st);
 }
 
 // ---------------------------------------------------------------------------
 // QueueToBitmap (gapbs-verify/bfs.cc:92-98, src/bfs.cc:104-112): set the bit
-// of every queue entry in `front` (all zero on entry).
-__global__ void __launch_bounds__(kThreads)
-k_q2b(const int32_t* __restrict__ qv, const DevCounters* __restrict__ ctr, int cur, int shift,
-      uint32_t* front) {
-  const int64_t F = (int64_t)(ctr->qpacked[cur] >> shift);
+// of every queue entry in the bottom-up frontier bm[parity] (all zero on
+// entry: BitmapToQueue clears what it reads, and the init clears bm0).
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_q2b(Bufs<OffT> b) {
+  DevState* st = b.st;
+  stamp_begin(st);
+  const int cur = st->cur;
+  const int32_t* qv = cur ? b.qv1 : b.qv0;
+  uint32_t* front = st->parity ? b.bm1 : b.bm0;
+  const int64_t F = (int64_t)(b.ctr->qpacked[cur] >> b.shift);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t v = qv[i];
     atomicOr(front + (v >> 5), 1u << (v & 31));
   }
+  stamp_end(st);
 }
 
 // ---------------------------------------------------------------------------
@@ -237,14 +388,23 @@ k_q2b(const int32_t* __restrict__ qv, const DevCounters* __restrict__ ctr, int c
 // probes the first kProbe neighbours of its own vertex; vertices still open
 // after that are then scanned by the whole warp, 32 neighbours per ballot,
 // with early exit.  The warp writes next[w] and visited[w] whole.
+// kParity fixes which bitmap is the frontier (two graph nodes, one per parity).
 constexpr int kProbe = 4;
 
-template <typename OffT, bool kInstrument>
-__global__ void __launch_bounds__(kThreads, 4)
-k_bu(int64_t W, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
-     uint32_t* __restrict__ visited, int32_t* __restrict__ parent, int32_t* __restrict__ depth,
-     const uint32_t* __restrict__ front, uint32_t* __restrict__ next,
-     DevCounters* __restrict__ ctr, int level) {
+template <typename OffT, int kParity>
+__global__ void __launch_bounds__(kThreads, 4) k_bu(Bufs<OffT> b) {
+  DevState* st = b.st;
+  stamp_begin(st);
+  const int level = st->level;
+  const bool instrument = st->instrument != 0;
+  int32_t* depth = st->want_depth ? b.depth : nullptr;
+  const uint32_t* __restrict__ front = kParity ? b.bm1 : b.bm0;
+  uint32_t* __restrict__ next = kParity ? b.bm0 : b.bm1;
+  const OffT* __restrict__ off = b.off;
+  const int32_t* __restrict__ nbr = b.nbr;
+  uint32_t* __restrict__ visited = b.visited;
+  int32_t* __restrict__ parent = b.parent;
+  const int64_t W = b.W;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -276,16 +436,16 @@ k_bu(int64_t W, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
         }
       }
       unsigned long long my_scan = 0;
-      if (kInstrument && mine) my_scan = found ? pos - rs + 1 : pos - rs;
+      if (instrument && mine) my_scan = found ? pos - rs + 1 : pos - rs;
       unsigned pend = __ballot_sync(kFull, mine && !found && pos < re);
       while (pend) {
         const int src = __ffs(pend) - 1;
         pend &= pend - 1;
-        const uint64_t b = shfl(pos, src);
+        const uint64_t bpos = shfl(pos, src);
         const uint64_t e = shfl(re, src);
         int32_t hit = -1;
         uint64_t hitpos = e;
-        for (uint64_t base = b; base < e; base += 32) {
+        for (uint64_t base = bpos; base < e; base += 32) {
           const uint64_t idx = base + lane;
           bool h = false;
           int32_t v = 0;
@@ -306,7 +466,7 @@ k_bu(int64_t W, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
             found = true;
             par = hit;
           }
-          if (kInstrument) my_scan += (hit >= 0 ? hitpos + 1 : e) - b;
+          if (instrument) my_scan += (hit >= 0 ? hitpos + 1 : e) - bpos;
         }
       }
       if (found) {
@@ -314,7 +474,7 @@ k_bu(int64_t W, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
         if (depth) depth[u] = level;
       }
       claimed_mask = __ballot_sync(kFull, found);
-      if (kInstrument) {
+      if (instrument) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) my_scan += __shfl_xor_sync(kFull, my_scan, o);
         scanned += my_scan;
@@ -337,23 +497,30 @@ k_bu(int64_t W, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
       a += red[0][i];
       s += red[1][i];
     }
-    if (a) atomicAdd(&ctr->awake, a);
-    if (kInstrument && s) atomicAdd(&ctr->scanned, s);
+    if (a) atomicAdd(&b.ctr->awake, a);
+    if (s) atomicAdd(&b.ctr->scanned, s);
   }
+  stamp_end(st);
 }
 
 // ---------------------------------------------------------------------------
 // BitmapToQueue (gapbs-verify/bfs.cc:100-112, src/bfs.cc:115-125): every set
-// bit of `front` becomes a queue entry (with its degree prefix) and `front`
-// is cleared on the way, so it is all-zero for the next QueueToBitmap.
-// Thread per word; one atomic per CTA-iteration.
+// bit of the frontier bm[parity] becomes an entry of queue `cur` (with its
+// degree prefix), and the bitmap is cleared on the way so it is all-zero for
+// the next QueueToBitmap.  Thread per word; one atomic per CTA-iteration.
 template <typename OffT>
-__global__ void __launch_bounds__(kThreads)
-k_b2q(int64_t W, const OffT* __restrict__ off, uint32_t* __restrict__ front,
-      int32_t* __restrict__ qv_out, OffT* __restrict__ qs_out, DevCounters* __restrict__ ctr,
-      int dst, int shift) {
+__global__ void __launch_bounds__(kThreads) k_b2q(Bufs<OffT> b) {
   __shared__ unsigned long long warp_tot[kWarpsPerCta];
   __shared__ unsigned long long cta_base;
+  DevState* st = b.st;
+  stamp_begin(st);
+  const int dst = st->cur;
+  uint32_t* front = st->parity ? b.bm1 : b.bm0;
+  int32_t* qv_out = dst ? b.qv1 : b.qv0;
+  OffT* qs_out = dst ? b.qs1 : b.qs0;
+  const OffT* __restrict__ off = b.off;
+  const int shift = b.shift;
+  const int64_t W = b.W;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const unsigned long long emask = (1ull << shift) - 1;
@@ -366,8 +533,8 @@ k_b2q(int64_t W, const OffT* __restrict__ off, uint32_t* __restrict__ front,
       if (bits) front[w] = 0;
     }
     unsigned long long degsum = 0;
-    for (uint32_t b = bits; b; b &= b - 1) {
-      const int64_t u = (w << 5) + (__ffs(b) - 1);
+    for (uint32_t x = bits; x; x &= x - 1) {
+      const int64_t u = (w << 5) + (__ffs(x) - 1);
       degsum += (unsigned long long)(off[u + 1] - off[u]);
     }
     // packed (count, degree sum) per thread; inclusive scan over the CTA
@@ -382,15 +549,15 @@ k_b2q(int64_t W, const OffT* __restrict__ off, uint32_t* __restrict__ front,
         warp_tot[i] = t;
         t += x;
       }
-      cta_base = t ? atomicAdd(&ctr->qpacked[dst], t) : 0;
+      cta_base = t ? atomicAdd(&b.ctr->qpacked[dst], t) : 0;
     }
     __syncthreads();
     if (bits) {
       const unsigned long long at = cta_base + warp_tot[wib] + inc - mine;
       uint64_t qpos = at >> shift;
       uint64_t epos = at & emask;
-      for (uint32_t b = bits; b; b &= b - 1) {
-        const int64_t u = (w << 5) + (__ffs(b) - 1);
+      for (uint32_t x = bits; x; x &= x - 1) {
+        const int64_t u = (w << 5) + (__ffs(x) - 1);
         qv_out[qpos] = (int32_t)u;
         qs_out[qpos] = (OffT)epos;
         qpos++;
@@ -399,6 +566,7 @@ k_b2q(int64_t W, const OffT* __restrict__ off, uint32_t* __restrict__ front,
     }
     __syncthreads();
   }
+  stamp_end(st);
 }
 
 // ---------------------------------------------------------------------------
@@ -418,9 +586,9 @@ __global__ void k_iso_mask(int64_t n, int64_t W, const OffT* __restrict__ off,
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < W;
        w += (int64_t)gridDim.x * blockDim.x) {
     uint32_t m = 0;
-    for (int b = 0; b < 32; b++) {
-      const int64_t u = (w << 5) + b;
-      if (u >= n || off[u + 1] == off[u]) m |= 1u << b;
+    for (int i = 0; i < 32; i++) {
+      const int64_t u = (w << 5) + i;
+      if (u >= n || off[u + 1] == off[u]) m |= 1u << i;
     }
     iso[w] = m;
   }

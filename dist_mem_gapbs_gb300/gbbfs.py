@@ -56,7 +56,8 @@ class Step(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("steps", ctypes.POINTER(Step)), ("max_steps", ctypes.c_int32),
-                ("instrument", ctypes.c_int32), ("num_steps", ctypes.c_int32),
+                ("instrument", ctypes.c_int32), ("stepped", ctypes.c_int32),
+                ("num_steps", ctypes.c_int32),
                 ("levels", ctypes.c_int32), ("device_ms", ctypes.c_double),
                 ("init_seconds", ctypes.c_double), ("reached", ctypes.c_int64),
                 ("alg_bytes", ctypes.c_int64)]
@@ -260,17 +261,18 @@ class SearchStats:
         return [(s["kind"], s["count"] if s["kind"] in ("td", "bu") else 0) for s in self.steps]
 
 
-def _stats_block(instrument, max_steps=4096):
+def _stats_block(instrument, stepped=False, max_steps=4096):
     steps = (Step * max_steps)()
     st = Stats()
     st.steps = ctypes.cast(steps, ctypes.POINTER(Step))
     st.max_steps = max_steps
     st.instrument = 1 if instrument else 0
+    st.stepped = 1 if stepped else 0
     return st, steps
 
 
 def DOBFS(g, source, alpha=15, beta=18, depth=False, stats=False, instrument=False,
-          parent_out=None, depth_out=None):
+          stepped=False, parent_out=None, depth_out=None):
     """One direction-optimizing BFS; returns parent (and depth, stats on request).
 
     parent uses the reference's output encoding: parent[source] == source and
@@ -280,7 +282,8 @@ def DOBFS(g, source, alpha=15, beta=18, depth=False, stats=False, instrument=Fal
     dep = None
     if depth:
         dep = depth_out if depth_out is not None else np.empty(g.n, dtype=np.int32)
-    st, steps = _stats_block(instrument) if (stats or instrument) else (None, None)
+    st, steps = (_stats_block(instrument, stepped) if (stats or instrument or stepped)
+                 else (None, None))
     _check(lib().gbbfs_bfs(g.handle, int(source), int(alpha), int(beta), _p(parent), _p(dep),
                            ctypes.byref(st) if st is not None else None), "bfs")
     out = [parent]
@@ -291,9 +294,11 @@ def DOBFS(g, source, alpha=15, beta=18, depth=False, stats=False, instrument=Fal
     return out[0] if len(out) == 1 else tuple(out)
 
 
-def bfs_device(g, source, alpha=15, beta=18, want_depth=False, stats=False, instrument=False):
+def bfs_device(g, source, alpha=15, beta=18, want_depth=False, stats=False, instrument=False,
+               stepped=False):
     """The search with results left in HBM; returns SearchStats or None."""
-    st, steps = _stats_block(instrument) if (stats or instrument) else (None, None)
+    st, steps = (_stats_block(instrument, stepped) if (stats or instrument or stepped)
+                 else (None, None))
     _check(lib().gbbfs_bfs_device(g.handle, int(source), int(alpha), int(beta),
                                   1 if want_depth else 0,
                                   ctypes.byref(st) if st is not None else None), "bfs_device")

@@ -59,6 +59,9 @@ typedef struct gbbfs_stats {
   gbbfs_step* steps;   /* caller array for the trace, may be NULL            */
   int32_t max_steps;   /* its capacity                                        */
   int32_t instrument;  /* 1: count scanned edges and algorithmic bytes (slower) */
+  int32_t stepped;     /* 1: host-stepped loop, CUDA events around every step
+                          kernel; 0: the whole search as one CUDA graph (step
+                          times then come from device timer stamps)         */
   /* out */
   int32_t num_steps;   /* records the search produced (may exceed max_steps) */
   int32_t levels;      /* number of BFS levels discovered                   */

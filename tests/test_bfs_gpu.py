@@ -45,6 +45,13 @@ def check_against_oracle(native, oracle, off, nbr, g, src, alpha=15, beta=18):
         if s["kind"] == "bu":
             assert s["unvisited"] == r["unvisited"]
     assert st.alg_bytes == ost["alg_bytes"]
+    # the host-stepped driver runs the same kernels and decisions
+    p2, d2, st2 = native.DOBFS(g, src, alpha=alpha, beta=beta, depth=True, stats=True,
+                               instrument=True, stepped=True)
+    assert np.array_equal(d2, depth)
+    assert st2.trace == st.trace
+    assert st2.alg_bytes == st.alg_bytes
+    assert all(s["seconds"] >= 0 for s in st2.steps)
     return parent, depth, st
 
 
