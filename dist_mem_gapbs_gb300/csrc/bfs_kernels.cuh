@@ -262,9 +262,19 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
   int staged = 0;
 
   auto flush = [&]() {
-    // One atomic for the whole stage: (count << shift) + summed degrees.
+    // Degrees of the staged claims, loaded together (8 independent loads per
+    // lane), then one atomic for the whole stage: (count << shift) + degrees.
     OffT red = 0;
-    for (int i = lane; i < staged; i += 32) red += st_d[wib][i];
+#pragma unroll
+    for (int q = 0; q < kTdStage / 32; q++) {
+      const int i = lane + 32 * q;
+      if (i < staged) {
+        const int32_t v = st_v[wib][i];
+        const OffT d = __ldg(off + v + 1) - __ldg(off + v);
+        st_d[wib][i] = d;
+        red += d;
+      }
+    }
 #pragma unroll
     for (int o = 16; o; o >>= 1) red += shfl(red, lane ^ o);
     unsigned long long base = 0;
@@ -297,15 +307,23 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
       if ((uint64_t)qs[mid] <= e0) lo = mid; else hi = mid - 1;
     }
     int64_t i0 = lo;
+    int64_t ij = -1;
+    uint64_t sj = ~0ull;
+    int32_t uj = 0;
+    uint64_t rj = 0;
     for (uint64_t c = c_begin; c < c_end; c++, e0 += 32) {
-      const int64_t ij = i0 + lane;
-      uint64_t sj = ~0ull;
-      int32_t uj = 0;
-      uint64_t rj = 0;
-      if (ij < F) {
-        sj = (uint64_t)qs[ij];
-        uj = qv[ij];
-        rj = (uint64_t)off[uj];
+      // The window of 32 queue entries from i0; unchanged while the walk
+      // stays inside one entry (a hub), so it is reloaded only when i0 moved.
+      if (ij != i0 + lane) {
+        ij = i0 + lane;
+        sj = ~0ull;
+        uj = 0;
+        rj = 0;
+        if (ij < F) {
+          sj = (uint64_t)qs[ij];
+          uj = qv[ij];
+          rj = (uint64_t)off[uj];
+        }
       }
       // Bit p set <=> a window entry starts at edge e0 + p (entry i0 covers e0).
       unsigned mybit = 0;
@@ -319,7 +337,6 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
       const uint64_t e = e0 + lane;
       bool claimed = false;
       int32_t v = 0;
-      OffT dv = 0;
       if (e < E) {
         v = __ldg(nbr + (r + (e - s)));
         const uint32_t bit = 1u << (v & 31);
@@ -330,7 +347,6 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
             claimed = true;
             b.parent[v] = u;
             if (depth) depth[v] = level;
-            dv = __ldg(off + v + 1) - __ldg(off + v);
           }
         }
       }
@@ -341,7 +357,6 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
         if (claimed) {
           const int slot = staged + __popc(cm & ((1u << lane) - 1));
           st_v[wib][slot] = v;
-          st_d[wib][slot] = dv;
         }
         staged += cnt;
         __syncwarp();
@@ -382,17 +397,22 @@ __global__ void __launch_bounds__(kThreads) k_q2b(Bufs<OffT> b) {
 // ---------------------------------------------------------------------------
 // Bottom-up step: BUStep (gapbs-verify/bfs.cc:46-64, src/bfs.cc:57-78).
 //
-// One warp per bitmap word.  Every unvisited vertex u of the word looks for
-// the FIRST neighbour (in sorted order) whose front bit is set, as the
-// reference does, so bottom-up parents equal the reference's.  Each lane first
-// probes the first kProbe neighbours of its own vertex; vertices still open
-// after that are then scanned by the whole warp, 32 neighbours per ballot,
-// with early exit.  The warp writes next[w] and visited[w] whole.
-// kParity fixes which bitmap is the frontier (two graph nodes, one per parity).
+// Every unvisited vertex u looks for the FIRST neighbour (in sorted order)
+// whose front bit is set, as the reference does, so bottom-up parents equal
+// the reference's.  A warp takes 32 consecutive bitmap words per iteration,
+// one word per lane (coalesced visited/next traffic, fully-visited words cost
+// one bit test):
+//  1. each lane walks the unvisited vertices of its own word and probes their
+//     first kProbe neighbours, all loads of a probe issued together, so a warp
+//     keeps 32 independent vertex chains in flight;
+//  2. vertices still open after the probe are scanned by the whole warp,
+//     32 neighbours per ballot, with early exit.
+// Each lane owns its word: next[w] and visited[w] are written whole, with no
+// atomics.  kParity fixes which bitmap is the frontier (two graph nodes).
 constexpr int kProbe = 4;
 
 template <typename OffT, int kParity>
-__global__ void __launch_bounds__(kThreads, 4) k_bu(Bufs<OffT> b) {
+__global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
   DevState* st = b.st;
   stamp_begin(st);
   const int level = st->level;
@@ -409,44 +429,57 @@ __global__ void __launch_bounds__(kThreads, 4) k_bu(Bufs<OffT> b) {
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   unsigned long long awake = 0, scanned = 0;
-  for (int64_t w = warp; w < W; w += nwarps) {
-    const uint32_t vis = visited[w];
-    const uint32_t unv = ~vis;
-    uint32_t claimed_mask = 0;
-    if (unv) {
-      const int64_t u = (w << 5) + lane;
-      const bool mine = (unv >> lane) & 1u;
-      uint64_t rs = 0, re = 0;
-      if (mine) {
-        rs = (uint64_t)off[u];
-        re = (uint64_t)off[u + 1];
+  for (int64_t base = warp << 5; base < W; base += nwarps << 5) {
+    const int64_t w = base + lane;
+    const bool valid = w < W;
+    const uint32_t vis = valid ? visited[w] : kFull;
+    uint32_t todo = ~vis;
+    uint32_t claimed = 0, pend = 0;
+    // 1. thread per vertex over my word
+    while (todo) {
+      const int j = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int64_t u = (w << 5) + j;
+      const uint64_t rs = (uint64_t)off[u];
+      const uint64_t re = (uint64_t)off[u + 1];
+      int32_t v[kProbe];
+#pragma unroll
+      for (int k = 0; k < kProbe; k++) v[k] = rs + k < re ? __ldg(nbr + rs + k) : -1;
+      uint32_t hits = 0;
+#pragma unroll
+      for (int k = 0; k < kProbe; k++)
+        if (v[k] >= 0 && ((__ldg(front + (v[k] >> 5)) >> (v[k] & 31)) & 1u)) hits |= 1u << k;
+      if (hits) {
+        const int k = __ffs(hits) - 1;
+        int32_t p = v[0];
+#pragma unroll
+        for (int q = 1; q < kProbe; q++) p = k == q ? v[q] : p;
+        parent[u] = p;
+        if (depth) depth[u] = level;
+        claimed |= 1u << j;
+        if (instrument) scanned += k + 1;
+      } else {
+        if (re > rs + kProbe) pend |= 1u << j;
+        if (instrument) scanned += re - rs < (uint64_t)kProbe ? re - rs : kProbe;
       }
-      uint64_t pos = rs;
-      int32_t par = -1;
-      bool found = false;
-      if (mine) {
-        const uint64_t stop = re < rs + kProbe ? re : rs + kProbe;
-        for (; pos < stop; pos++) {
-          const int32_t v = __ldg(nbr + pos);
-          if ((__ldg(front + (v >> 5)) >> (v & 31)) & 1u) {
-            par = v;
-            found = true;
-            break;
-          }
-        }
-      }
-      unsigned long long my_scan = 0;
-      if (instrument && mine) my_scan = found ? pos - rs + 1 : pos - rs;
-      unsigned pend = __ballot_sync(kFull, mine && !found && pos < re);
-      while (pend) {
-        const int src = __ffs(pend) - 1;
-        pend &= pend - 1;
-        const uint64_t bpos = shfl(pos, src);
-        const uint64_t e = shfl(re, src);
+    }
+    // 2. the whole warp on each vertex still open
+    unsigned lanes = __ballot_sync(kFull, pend != 0);
+    while (lanes) {
+      const int t = __ffs(lanes) - 1;
+      lanes &= lanes - 1;
+      uint32_t pm = __shfl_sync(kFull, pend, t);
+      const int64_t wt = base + t;
+      while (pm) {
+        const int j = __ffs(pm) - 1;
+        pm &= pm - 1;
+        const int64_t u = (wt << 5) + j;
+        const uint64_t bpos = (uint64_t)off[u] + kProbe;
+        const uint64_t e = (uint64_t)off[u + 1];
         int32_t hit = -1;
         uint64_t hitpos = e;
-        for (uint64_t base = bpos; base < e; base += 32) {
-          const uint64_t idx = base + lane;
+        for (uint64_t p0 = bpos; p0 < e; p0 += 32) {
+          const uint64_t idx = p0 + lane;
           bool h = false;
           int32_t v = 0;
           if (idx < e) {
@@ -457,34 +490,32 @@ __global__ void __launch_bounds__(kThreads, 4) k_bu(Bufs<OffT> b) {
           if (hb) {
             const int first = __ffs(hb) - 1;
             hit = __shfl_sync(kFull, v, first);
-            hitpos = base + first;
+            hitpos = p0 + first;
             break;
           }
         }
-        if (lane == src) {
-          if (hit >= 0) {
-            found = true;
-            par = hit;
+        if (hit >= 0) {
+          if (lane == 0) {
+            parent[u] = hit;
+            if (depth) depth[u] = level;
           }
-          if (instrument) my_scan += (hit >= 0 ? hitpos + 1 : e) - bpos;
+          if (lane == t) claimed |= 1u << j;
         }
+        if (instrument && lane == 0) scanned += (hit >= 0 ? hitpos + 1 : e) - bpos;
       }
-      if (found) {
-        parent[u] = par;
-        if (depth) depth[u] = level;
-      }
-      claimed_mask = __ballot_sync(kFull, found);
-      if (instrument) {
-#pragma unroll
-        for (int o = 16; o; o >>= 1) my_scan += __shfl_xor_sync(kFull, my_scan, o);
-        scanned += my_scan;
-      }
-      if (lane == 0 && claimed_mask) visited[w] = vis | claimed_mask;
-      awake += __popc(claimed_mask);
     }
-    if (lane == 0) next[w] = claimed_mask;
+    if (valid) {
+      next[w] = claimed;
+      if (claimed) visited[w] = vis | claimed;
+    }
+    awake += __popc(claimed);
   }
   // One atomic per CTA.
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    awake += __shfl_xor_sync(kFull, awake, o);
+    scanned += __shfl_xor_sync(kFull, scanned, o);
+  }
   __shared__ unsigned long long red[2][kWarpsPerCta];
   if (lane == 0) {
     red[0][threadIdx.x >> 5] = awake;
