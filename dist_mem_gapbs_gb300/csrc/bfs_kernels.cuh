@@ -229,6 +229,7 @@ __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
 // falls out of the packed queue counter.  Claims are staged per warp in
 // shared memory and appended with one atomic per 256 claims.
 constexpr int kTdStage = 256;
+constexpr int kHub = 4;   // chunks per group on the hub fast path
 
 template <typename OffT>
 __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
@@ -297,6 +298,17 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
     __syncwarp();
     staged = 0;
   };
+  // Append this lane's claim (if any) to the warp's stage.
+  auto stage = [&](bool claimed, int32_t v) {
+    const unsigned cm = __ballot_sync(kFull, claimed);
+    if (cm) {
+      const int cnt = __popc(cm);
+      if (staged + cnt > kTdStage) flush();
+      if (claimed) st_v[wib][staged + __popc(cm & ((1u << lane) - 1))] = v;
+      staged += cnt;
+      __syncwarp();
+    }
+  };
 
   if (c_begin < c_end) {
     uint64_t e0 = c_begin << 5;
@@ -325,6 +337,41 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
           rj = (uint64_t)off[uj];
         }
       }
+      // Hub fast path: when entry i0 covers the next kHub chunks, process them
+      // together, every load of the group issued before any of them is used.
+      const uint64_t s_next = shfl(sj, 1);   // first edge of entry i0 + 1
+      if (c + kHub <= c_end && s_next >= e0 + 32 * kHub) {
+        const int32_t u = __shfl_sync(kFull, uj, 0);
+        const uint64_t base_nb = shfl(rj, 0) + (e0 - shfl(sj, 0)) + lane;
+        int32_t v[kHub];
+        uint32_t w[kHub];
+#pragma unroll
+        for (int q = 0; q < kHub; q++)
+          v[q] = e0 + 32 * q + lane < E ? __ldg(nbr + base_nb + 32 * q) : -1;
+#pragma unroll
+        for (int q = 0; q < kHub; q++) w[q] = v[q] >= 0 ? __ldcg(visited + (v[q] >> 5)) : kFull;
+        bool cl[kHub];
+#pragma unroll
+        for (int q = 0; q < kHub; q++) {
+          cl[q] = false;
+          if (v[q] >= 0 && !(w[q] & (1u << (v[q] & 31)))) {
+            const uint32_t bit = 1u << (v[q] & 31);
+            cl[q] = !(atomicOr(visited + (v[q] >> 5), bit) & bit);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < kHub; q++) {
+          if (cl[q]) {
+            b.parent[v[q]] = u;
+            if (depth) depth[v[q]] = level;
+          }
+          stage(cl[q], v[q]);
+        }
+        if (s_next == e0 + 32 * kHub) i0 += 1;
+        c += kHub - 1;
+        e0 += 32 * (kHub - 1);
+        continue;
+      }
       // Bit p set <=> a window entry starts at edge e0 + p (entry i0 covers e0).
       unsigned mybit = 0;
       if (lane == 0) mybit = 1u;
@@ -350,17 +397,7 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
           }
         }
       }
-      const unsigned cm = __ballot_sync(kFull, claimed);
-      if (cm) {
-        const int cnt = __popc(cm);
-        if (staged + cnt > kTdStage) flush();
-        if (claimed) {
-          const int slot = staged + __popc(cm & ((1u << lane) - 1));
-          st_v[wib][slot] = v;
-        }
-        staged += cnt;
-        __syncwarp();
-      }
+      stage(claimed, v);
       // Advance to the entry that covers edge e0 + 32.  The window holds 32
       // entries; when all of them start at or before e0 + 32, entry i0 + 32
       // may start exactly there.
@@ -401,18 +438,21 @@ __global__ void __launch_bounds__(kThreads) k_q2b(Bufs<OffT> b) {
 // whose front bit is set, as the reference does, so bottom-up parents equal
 // the reference's.  A warp takes 32 consecutive bitmap words per iteration,
 // one word per lane (coalesced visited/next traffic, fully-visited words cost
-// one bit test):
-//  1. each lane walks the unvisited vertices of its own word and probes their
-//     first kProbe neighbours, all loads of a probe issued together, so a warp
-//     keeps 32 independent vertex chains in flight;
-//  2. vertices still open after the probe are scanned by the whole warp,
-//     32 neighbours per ballot, with early exit.
-// Each lane owns its word: next[w] and visited[w] are written whole, with no
-// atomics.  kParity fixes which bitmap is the frontier (two graph nodes).
-constexpr int kProbe = 4;
+// one bit test).  The unvisited vertices of those 32 words form a pool in
+// shared memory; every lane scans one vertex at a time, kBatch neighbours per
+// round with all loads of a round issued together, and takes the next vertex
+// from the pool as soon as its own is resolved.  So a warp keeps 32
+// independent scans in flight whatever the degrees, and reads at most
+// kBatch - 1 neighbours past the first hit.  Claims are gathered per word in
+// shared memory; the lane that owns a word then writes next[w] and
+// visited[w] whole, with no global atomics.  kParity fixes which bitmap is the
+// frontier (two graph nodes).
+constexpr int kBatch = 8;
 
 template <typename OffT, int kParity>
 __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
+  __shared__ uint16_t pool[kWarpsPerCta][1024];
+  __shared__ uint32_t got[kWarpsPerCta][32];
   DevState* st = b.st;
   stamp_begin(st);
   const int level = st->level;
@@ -426,89 +466,84 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
   int32_t* __restrict__ parent = b.parent;
   const int64_t W = b.W;
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  uint16_t* my_pool = pool[wib];
   unsigned long long awake = 0, scanned = 0;
   for (int64_t base = warp << 5; base < W; base += nwarps << 5) {
     const int64_t w = base + lane;
     const bool valid = w < W;
     const uint32_t vis = valid ? visited[w] : kFull;
     uint32_t todo = ~vis;
-    uint32_t claimed = 0, pend = 0;
-    // 1. thread per vertex over my word
-    while (todo) {
+    // Pool of this chunk's unvisited vertices (chunk-local index 32*lane + bit),
+    // word by word, so lanes that start together read neighbouring offsets.
+    const int cnt = __popc(todo);
+    const int incl = warp_inclusive_sum(cnt, lane);
+    const int total = __shfl_sync(kFull, incl, 31);
+    got[wib][lane] = 0;
+    if (total == 0) {
+      if (valid) next[w] = 0;
+      continue;
+    }
+    for (int k = incl - cnt; todo; k++) {
       const int j = __ffs(todo) - 1;
       todo &= todo - 1;
-      const int64_t u = (w << 5) + j;
-      const uint64_t rs = (uint64_t)off[u];
-      const uint64_t re = (uint64_t)off[u + 1];
-      int32_t v[kProbe];
-#pragma unroll
-      for (int k = 0; k < kProbe; k++) v[k] = rs + k < re ? __ldg(nbr + rs + k) : -1;
-      uint32_t hits = 0;
-#pragma unroll
-      for (int k = 0; k < kProbe; k++)
-        if (v[k] >= 0 && ((__ldg(front + (v[k] >> 5)) >> (v[k] & 31)) & 1u)) hits |= 1u << k;
-      if (hits) {
-        const int k = __ffs(hits) - 1;
-        int32_t p = v[0];
-#pragma unroll
-        for (int q = 1; q < kProbe; q++) p = k == q ? v[q] : p;
-        parent[u] = p;
-        if (depth) depth[u] = level;
-        claimed |= 1u << j;
-        if (instrument) scanned += k + 1;
-      } else {
-        if (re > rs + kProbe) pend |= 1u << j;
-        if (instrument) scanned += re - rs < (uint64_t)kProbe ? re - rs : kProbe;
-      }
+      my_pool[k] = (uint16_t)((lane << 5) | j);
     }
-    // 2. the whole warp on each vertex still open
-    unsigned lanes = __ballot_sync(kFull, pend != 0);
-    while (lanes) {
-      const int t = __ffs(lanes) - 1;
-      lanes &= lanes - 1;
-      uint32_t pm = __shfl_sync(kFull, pend, t);
-      const int64_t wt = base + t;
-      while (pm) {
-        const int j = __ffs(pm) - 1;
-        pm &= pm - 1;
-        const int64_t u = (wt << 5) + j;
-        const uint64_t bpos = (uint64_t)off[u] + kProbe;
-        const uint64_t e = (uint64_t)off[u + 1];
-        int32_t hit = -1;
-        uint64_t hitpos = e;
-        for (uint64_t p0 = bpos; p0 < e; p0 += 32) {
-          const uint64_t idx = p0 + lane;
-          bool h = false;
-          int32_t v = 0;
-          if (idx < e) {
-            v = __ldg(nbr + idx);
-            h = (__ldg(front + (v >> 5)) >> (v & 31)) & 1u;
-          }
-          const unsigned hb = __ballot_sync(kFull, h);
-          if (hb) {
-            const int first = __ffs(hb) - 1;
-            hit = __shfl_sync(kFull, v, first);
-            hitpos = p0 + first;
-            break;
+    __syncwarp();
+    int taken = 0;           // pool entries handed out (warp-uniform)
+    int item = -1;           // chunk-local index of my vertex, -1 when idle
+    uint64_t pos = 0, end = 0, start = 0;
+    for (;;) {
+      const unsigned needy = __ballot_sync(kFull, item < 0);
+      if (item < 0) {
+        const int idx = taken + __popc(needy & ((1u << lane) - 1));
+        if (idx < total) {
+          item = my_pool[idx];
+          const int64_t u = ((base + (item >> 5)) << 5) + (item & 31);
+          start = pos = (uint64_t)off[u];
+          end = (uint64_t)off[u + 1];
+        }
+      }
+      taken += __popc(needy);
+      if (!__any_sync(kFull, item >= 0)) break;
+      if (item >= 0) {
+        int32_t v[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; k++) v[k] = pos + k < end ? __ldg(nbr + pos + k) : -1;
+        uint32_t hits = 0;
+#pragma unroll
+        for (int k = 0; k < kBatch; k++)
+          if (v[k] >= 0 && ((__ldg(front + (v[k] >> 5)) >> (v[k] & 31)) & 1u)) hits |= 1u << k;
+        if (hits) {
+          const int k = __ffs(hits) - 1;
+          int32_t p = v[0];
+#pragma unroll
+          for (int q = 1; q < kBatch; q++) p = k == q ? v[q] : p;
+          const int64_t u = ((base + (item >> 5)) << 5) + (item & 31);
+          parent[u] = p;
+          if (depth) depth[u] = level;
+          atomicOr(&got[wib][item >> 5], 1u << (item & 31));
+          if (instrument) scanned += pos + k + 1 - start;
+          item = -1;
+        } else {
+          pos += kBatch;
+          if (pos >= end) {
+            if (instrument) scanned += end - start;
+            item = -1;
           }
         }
-        if (hit >= 0) {
-          if (lane == 0) {
-            parent[u] = hit;
-            if (depth) depth[u] = level;
-          }
-          if (lane == t) claimed |= 1u << j;
-        }
-        if (instrument && lane == 0) scanned += (hit >= 0 ? hitpos + 1 : e) - bpos;
       }
     }
+    __syncwarp();
+    const uint32_t claimed = got[wib][lane];
     if (valid) {
       next[w] = claimed;
       if (claimed) visited[w] = vis | claimed;
     }
     awake += __popc(claimed);
+    __syncwarp();
   }
   // One atomic per CTA.
 #pragma unroll
