@@ -40,7 +40,7 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbbfs", choices=["gbbfs", "reference"])
-    ap.add_argument("--graph", default="g22", choices=sorted(GRAPHS))
+    ap.add_argument("--graph", default="g26", choices=sorted(GRAPHS))
     ap.add_argument("--sources", type=int, default=64)
     ap.add_argument("--cpu-budget-s", type=float, default=20.0,
                     help="bound on the CPU-baseline sample")
