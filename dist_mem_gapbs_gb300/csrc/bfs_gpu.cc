@@ -14,6 +14,9 @@
 //   --output <path>          file for -v (default bfs_output.txt)
 //   --dmm-format             prefix every line with "PE: 0 | "
 //   --sg-out <path>          write the built graph as a .sg serialized graph
+//   --stepped                drive each search step by step from the host
+//                            (CUDA events around every step kernel) instead of
+//                            one CUDA graph launch per search
 
 #include <getopt.h>
 
@@ -62,6 +65,7 @@ struct Options {
   int alpha = 15, beta = 18;
   std::string output = "bfs_output.txt";
   std::string sg_out;
+  bool stepped = false;
 };
 
 void Usage(const char* name) {
@@ -82,7 +86,7 @@ void Usage(const char* name) {
   line('n', "n", "perform n trials", "16");
   line('r', "node", "start from node r", "rand");
   line('v', "", "verify the output of each run", "false");
-  printf("    --alpha <a> --beta <b> --output <path> --dmm-format --sg-out <path>\n");
+  printf("    --alpha <a> --beta <b> --output <path> --dmm-format --sg-out <path> --stepped\n");
   exit(0);
 }
 
@@ -93,6 +97,7 @@ bool ParseArgs(int argc, char** argv, Options* o) {
       {"output", required_argument, nullptr, 1002},
       {"dmm-format", no_argument, nullptr, 1003},
       {"sg-out", required_argument, nullptr, 1004},
+      {"stepped", no_argument, nullptr, 1005},
       {nullptr, 0, nullptr, 0}};
   int c;
   while ((c = getopt_long(argc, argv, "f:g:hk:su:an:r:v", longs, nullptr)) != -1) {
@@ -112,6 +117,7 @@ bool ParseArgs(int argc, char** argv, Options* o) {
       case 1002: o->output = optarg; break;
       case 1003: g_dmm = true; break;
       case 1004: o->sg_out = optarg; break;
+      case 1005: o->stepped = true; break;
       default: return false;
     }
   }
@@ -175,6 +181,7 @@ int main(int argc, char** argv) {
     memset(&st, 0, sizeof st);
     st.steps = steps.data();
     st.max_steps = (int32_t)steps.size();
+    st.stepped = o.stepped ? 1 : 0;
     const int32_t src = sources[t];
     rc = gbbfs_bfs(g, src, o.alpha, o.beta, parent.data(), nullptr, &st);
     if (rc != GBBFS_OK) {
