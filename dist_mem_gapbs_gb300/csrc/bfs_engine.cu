@@ -262,8 +262,9 @@ int create(const int64_t* offsets, const int32_t* neigh, int64_t n, int64_t m,
   GB_TRY(dev_alloc(g, &g->st, 1));
   GB_CUDA(cudaHostAlloc(&g->h_st, sizeof(DevState), cudaHostAllocDefault));
   memset(g->h_st, 0, sizeof(DevState));
+  g->h_st->t0 = ~0ull;  // kernel stamps take the min start / max end
   GB_CUDA(cudaMemsetAsync(g->ctr, 0, sizeof(DevCounters), g->stream));
-  GB_CUDA(cudaMemsetAsync(g->st, 0, sizeof(DevState), g->stream));
+  GB_CUDA(cudaMemcpyAsync(g->st, g->h_st, sizeof(DevState), cudaMemcpyHostToDevice, g->stream));
   if (g->off32) return upload<uint32_t>(g, offsets, neigh);
   return upload<unsigned long long>(g, offsets, neigh);
 }

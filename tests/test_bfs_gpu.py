@@ -52,6 +52,9 @@ def check_against_oracle(native, oracle, off, nbr, g, src, alpha=15, beta=18):
     assert st2.trace == st.trace
     assert st2.alg_bytes == st.alg_bytes
     assert all(s["seconds"] >= 0 for s in st2.steps)
+    for x in (st, st2):
+        assert 0 <= x.init_seconds < 1.0
+        assert all(0 <= s["seconds"] < 1.0 for s in x.steps)
     return parent, depth, st
 
 
@@ -141,8 +144,9 @@ def test_isolated_source_and_single_vertex(native, oracle):
         assert np.array_equal(depth, exp)
     off = np.zeros(2, np.int64)
     with native.Graph(off, np.zeros(0, np.int32)) as g:
-        parent = native.DOBFS(g, 0)
+        parent, st = native.DOBFS(g, 0, stats=True)
         assert list(parent) == [0]
+        assert 0 <= st.init_seconds < 1.0   # first search on a fresh handle
 
 
 def test_bad_source_rejected(native):
