@@ -26,30 +26,14 @@
 #include <vector>
 
 #include "bfs_kernels.cuh"
+#include "engine.h"
 #include "gbbfs.h"
 
 using namespace gbbfs;
 
 namespace {
 
-thread_local std::string g_last_error;
-
-#define GB_CUDA(call)                                                         \
-  do {                                                                        \
-    cudaError_t err_ = (call);                                                \
-    if (err_ != cudaSuccess) {                                                \
-      g_last_error = std::string(#call) + ": " + cudaGetErrorString(err_);    \
-      return GBBFS_ERR_CUDA;                                                  \
-    }                                                                         \
-  } while (0)
-
-#define GB_TRY(x)            \
-  do {                       \
-    int st_ = (x);           \
-    if (st_ != GBBFS_OK) {   \
-      return st_;            \
-    }                        \
-  } while (0)
+#define g_last_error (::gbbfs::last_error())
 
 int bit_length(uint64_t x) {
   int b = 0;
@@ -66,41 +50,14 @@ constexpr size_t kReadbackBytes = kHeaderBytes + kTraceInline * sizeof(DevStep);
 
 }  // namespace
 
-struct gbbfs_graph {
-  int64_t n = 0, m = 0, W = 0;
-  bool off32 = true;
-  int shift = 32;           // packed queue counter: (count << shift) | edges
-  int device = 0;
-  int sms = 0;
-  void* off = nullptr;      // uint32_t* or unsigned long long*
-  int32_t* nbr = nullptr;
-  uint32_t* iso = nullptr;
-  uint32_t* visited = nullptr;
-  uint32_t* bm[2] = {nullptr, nullptr};
-  int32_t* parent = nullptr;
-  int32_t* depth = nullptr;
-  int32_t* qv[2] = {nullptr, nullptr};
-  void* qs[2] = {nullptr, nullptr};
-  DevCounters* ctr = nullptr;
-  DevState* st = nullptr;
-  DevState* h_st = nullptr;       // pinned mirror (params in, header + trace out)
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
-  std::vector<cudaEvent_t> step_ev;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  int grid_init = 0, grid_td = 0, grid_bu = 0, grid_q2b = 0, grid_b2q = 0;
-  int64_t device_bytes = 0;
-  bool have_result = false;
-  bool result_depth = false;
-};
-
 namespace {
 
 void release(gbbfs_graph* g) {
   if (!g) return;
   if (g->device >= 0) cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
+  msbfs_release(g->ms);
+  g->ms = nullptr;
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->off);

@@ -1,0 +1,72 @@
+// Internal host-side definitions shared by the translation units of libgbbfs:
+// the graph handle, error reporting and the CUDA-call helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bfs_common.cuh"
+#include "gbbfs.h"
+
+namespace gbbfs {
+
+// Detail of the last failure on the calling thread (gbbfs_last_error).
+inline std::string& last_error() {
+  thread_local std::string msg;
+  return msg;
+}
+
+struct MsState;   // multi-source BFS buffers of a handle (msbfs.cu)
+void msbfs_release(MsState* ms);
+
+}  // namespace gbbfs
+
+#define GB_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t err_ = (call);                                                     \
+    if (err_ != cudaSuccess) {                                                     \
+      ::gbbfs::last_error() = std::string(#call) + ": " + cudaGetErrorString(err_); \
+      return GBBFS_ERR_CUDA;                                                       \
+    }                                                                              \
+  } while (0)
+
+#define GB_TRY(x)            \
+  do {                       \
+    int st_ = (x);           \
+    if (st_ != GBBFS_OK) {   \
+      return st_;            \
+    }                        \
+  } while (0)
+
+struct gbbfs_graph {
+  int64_t n = 0, m = 0, W = 0;
+  bool off32 = true;
+  int shift = 32;           // packed queue counter: (count << shift) | edges
+  int device = 0;
+  int sms = 0;
+  void* off = nullptr;      // uint32_t* or unsigned long long*
+  int32_t* nbr = nullptr;
+  uint32_t* iso = nullptr;
+  uint32_t* visited = nullptr;
+  uint32_t* bm[2] = {nullptr, nullptr};
+  int32_t* parent = nullptr;
+  int32_t* depth = nullptr;
+  int32_t* qv[2] = {nullptr, nullptr};
+  void* qs[2] = {nullptr, nullptr};
+  gbbfs::DevCounters* ctr = nullptr;
+  gbbfs::DevState* st = nullptr;
+  gbbfs::DevState* h_st = nullptr;  // pinned mirror (params in, header + trace out)
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  std::vector<cudaEvent_t> step_ev;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int grid_init = 0, grid_td = 0, grid_bu = 0, grid_q2b = 0, grid_b2q = 0;
+  int64_t device_bytes = 0;
+  bool have_result = false;
+  bool result_depth = false;
+  gbbfs::MsState* ms = nullptr;
+};

@@ -1,0 +1,725 @@
+// Batched multi-source BFS: up to 64 sources per batch as a bitmask per vertex.
+//
+// This form has no counterpart in the reference: it answers many BFS queries
+// of the same graph at once.  Its results are defined by the reference's
+// single-source search (src/bfs.cc:142-188): depth[s][v] equals the depth that
+// a plain DOBFS from source s gives vertex v, bit for bit.
+//
+// Layout in HBM (n vertices, L = lane word, 32 or 64 bits):
+//   visit  L[n]   bit i set once source i has reached v
+//   fr     L[n]   bit i set if v is in the frontier of source i
+//   acc    L[n]   bits found for v in the level being expanded
+//   q0/q1  int32  vertices with fr != 0 (current / next), degree sums packed
+//   tq     int32  vertices that received bits in this level
+//   depth  D[k][n] per-source depth (uint8 with 255 = unreached, or int32
+//                 with -1), written directly in [source][vertex] order
+//
+// One persistent cooperative kernel runs all levels of a batch.  Per level it
+// picks a direction from the frontier's summed degree (top-down below
+// m / alpha, bottom-up above, alpha chosen by the autotuner):
+//   top-down: warp per frontier vertex, atomicOr of fr[u] & ~visit[v] into
+//             acc[v]; the first writer of a vertex queues it;
+//   bottom-up: thread per unfinished vertex, OR of fr[u] over its neighbours,
+//             stopping once every lane of v is found; depth written in place,
+//             coalesced per source.
+// Then the old frontier is cleared and the new one (acc) is installed.  Grid
+// barriers between the phases spin on a generation word with a time bound
+// (%globaltimer); a barrier that runs out sets an error word and every block
+// returns, so the host gets GBBFS_ERR_TIMEOUT instead of a hung GPU.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "engine.h"
+
+namespace gbbfs {
+
+struct MsCtl {
+  unsigned long long q_packed[2];   // (count << shift) | summed degrees, per queue
+  unsigned long long touched[2];    // vertices queued in tq, per level parity
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int error;
+  int levels;
+  unsigned long long t_begin, t_end;
+};
+
+struct MsConfig {
+  int lanes = 64;        // 32 or 64 sources per batch
+  int batch = 8;         // neighbours per bottom-up round of one thread
+  int alpha = 15;        // top-down while frontier degrees <= m / alpha
+};
+
+struct MsState {
+  int64_t n = 0;
+  int depth_bytes = 0;
+  int lanes = 0;
+  void* visit = nullptr;
+  void* fr = nullptr;
+  void* acc = nullptr;
+  int32_t* q[2] = {nullptr, nullptr};
+  int32_t* tq = nullptr;
+  void* depth[2] = {nullptr, nullptr};
+  int32_t* d_src[2] = {nullptr, nullptr};
+  int32_t* h_src = nullptr;          // pinned, 2 x 64
+  MsCtl* ctl[2] = {nullptr, nullptr};
+  MsCtl* h_ctl = nullptr;            // pinned, 2
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t computed[2] = {nullptr, nullptr};
+  cudaEvent_t copied[2] = {nullptr, nullptr};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  MsConfig cfg;
+  MsConfig exec_cfg;
+  int exec_k[2] = {-1, -1};
+  int grid = 0;
+  int64_t bytes = 0;
+  int last_buf = -1;
+  int last_k = 0;
+};
+
+void msbfs_release(MsState* ms) {
+  if (!ms) return;
+  for (int i = 0; i < 2; i++) {
+    if (ms->exec[i]) cudaGraphExecDestroy(ms->exec[i]);
+    cudaFree(ms->q[i]);
+    cudaFree(ms->depth[i]);
+    cudaFree(ms->d_src[i]);
+    cudaFree(ms->ctl[i]);
+    if (ms->computed[i]) cudaEventDestroy(ms->computed[i]);
+    if (ms->copied[i]) cudaEventDestroy(ms->copied[i]);
+  }
+  cudaFree(ms->visit);
+  cudaFree(ms->fr);
+  cudaFree(ms->acc);
+  cudaFree(ms->tq);
+  if (ms->h_src) cudaFreeHost(ms->h_src);
+  if (ms->h_ctl) cudaFreeHost(ms->h_ctl);
+  if (ms->ev0) cudaEventDestroy(ms->ev0);
+  if (ms->ev1) cudaEventDestroy(ms->ev1);
+  if (ms->copy_stream) cudaStreamDestroy(ms->copy_stream);
+  delete ms;
+}
+
+// ---------------------------------------------------------------------------
+// Device side.
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT atomic_or_lane(LaneT* p, LaneT v) {
+  if constexpr (sizeof(LaneT) == 8)
+    return (LaneT)atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+  else
+    return (LaneT)atomicOr(reinterpret_cast<unsigned int*>(p), (unsigned int)v);
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
+  if constexpr (sizeof(LaneT) == 8)
+    return (LaneT)__ldcg(reinterpret_cast<const unsigned long long*>(p));
+  else
+    return (LaneT)__ldcg(reinterpret_cast<const unsigned int*>(p));
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT warp_or(LaneT x) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x |= shfl(x, (int)(threadIdx.x & 31) ^ o);
+  return x;
+}
+
+// Grid-wide barrier with a time bound.  Returns false (and every later call
+// returns false at once) when any block has given up.
+__device__ __forceinline__ bool grid_barrier(MsCtl* c, unsigned nblocks,
+                                             unsigned long long limit_ns) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned* vgen = &c->bar_gen;
+    const unsigned gen = *vgen;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == nblocks - 1) {
+      c->bar_count = 0;
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer();
+      while (*vgen == gen) {
+        if (*(volatile int*)&c->error) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer() - t0 > limit_ns) {
+          atomicExch(&c->error, GBBFS_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)&c->error) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <typename OffT, typename LaneT, typename DepthT>
+struct MsArgs {
+  const OffT* off;
+  const int32_t* nbr;
+  int64_t n, m;
+  LaneT* visit;
+  LaneT* fr;
+  LaneT* acc;
+  int32_t* q0;
+  int32_t* q1;
+  int32_t* tq;
+  DepthT* depth;
+  const int32_t* sources;
+  MsCtl* ctl;
+  int k;
+  int shift;
+  int alpha;
+  unsigned long long limit_ns;
+};
+
+// Write depth `level` for every source bit of `nb` at vertex v.  Called by a
+// whole warp; lanes with consecutive v write consecutive bytes per source.
+template <typename LaneT, typename DepthT>
+__device__ __forceinline__ void write_depths(DepthT* depth, int64_t n, int64_t v, LaneT nb,
+                                             int level) {
+  LaneT any = warp_or(nb);
+  while (any) {
+    const int i = (sizeof(LaneT) == 8) ? __ffsll((long long)any) - 1 : __ffs((int)any) - 1;
+    any &= any - 1;
+    if ((nb >> i) & 1) depth[(int64_t)i * n + v] = (DepthT)level;
+  }
+}
+
+template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
+__global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
+  MsCtl* c = a.ctl;
+  const unsigned nblocks = gridDim.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int64_t warp = tid >> 5;
+  const int64_t nwarps = nthreads >> 5;
+  const unsigned long long emask = (1ull << a.shift) - 1;
+  const LaneT all = a.k >= (int)(8 * sizeof(LaneT)) ? (LaneT)~(LaneT)0
+                                                     : (LaneT)(((LaneT)1 << a.k) - 1);
+  const int max_level = sizeof(DepthT) == 1 ? 254 : 0x7ffffffe;
+  if (tid == 0) c->t_begin = globaltimer();
+
+  // Sources: lane i starts at sources[i] (depth 0).  A vertex that is the
+  // source of several lanes is queued once.
+  if (blockIdx.x == 0 && threadIdx.x < a.k) {
+    const int i = threadIdx.x;
+    const int32_t s = a.sources[i];
+    const LaneT bit = (LaneT)1 << i;
+    atomic_or_lane(a.visit + s, bit);
+    a.depth[(int64_t)i * a.n + s] = 0;
+    if (atomic_or_lane(a.fr + s, bit) == 0) {
+      const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
+      const unsigned long long at =
+          atomicAdd(&c->q_packed[0], (1ull << a.shift) + deg) >> a.shift;
+      a.q0[at] = s;
+    }
+  }
+  if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+
+  int cur = 0;
+  for (int level = 1;; level++) {
+    const unsigned long long p = __ldcg(&c->q_packed[cur]);
+    const int64_t F = (int64_t)(p >> a.shift);
+    const uint64_t E = p & emask;
+    if (F == 0) break;
+    if (level > max_level) {
+      if (tid == 0) atomicExch(&c->error, GBBFS_ERR_ARG);
+      break;
+    }
+    const int32_t* q = cur ? a.q1 : a.q0;
+    int32_t* qn = cur ? a.q0 : a.q1;
+    unsigned long long* touched = &c->touched[level & 1];
+    const bool bottom_up = E > (uint64_t)(a.m / a.alpha);
+
+    if (!bottom_up) {
+      // Top-down: warp per frontier vertex.
+      for (int64_t i = warp; i < F; i += nwarps) {
+        const int32_t u = q[i];
+        const LaneT f = ld_lane(a.fr + u);
+        const uint64_t b0 = (uint64_t)a.off[u], b1 = (uint64_t)a.off[u + 1];
+        for (uint64_t e0 = b0; e0 < b1; e0 += 32) {
+          const uint64_t e = e0 + lane;
+          bool first = false;
+          int32_t v = 0;
+          if (e < b1) {
+            v = __ldg(a.nbr + e);
+            const LaneT nb = f & ~ld_lane(a.visit + v);
+            if (nb) first = atomic_or_lane(a.acc + v, nb) == 0;
+          }
+          const unsigned fm = __ballot_sync(kFull, first);
+          if (fm) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(touched, (unsigned long long)__popc(fm));
+            base = shfl(base, 0);
+            if (first) a.tq[base + __popc(fm & ((1u << lane) - 1))] = v;
+          }
+        }
+      }
+    } else {
+      // Bottom-up: thread per vertex, all lanes of v at once.
+      for (int64_t v0 = warp << 5; v0 < a.n; v0 += nwarps << 5) {
+        const int64_t v = v0 + lane;
+        LaneT nb = 0;
+        if (v < a.n) {
+          const LaneT vis = ld_lane(a.visit + v);
+          if (vis != all) {
+            uint64_t pos = (uint64_t)a.off[v];
+            const uint64_t end = (uint64_t)a.off[v + 1];
+            LaneT got = 0;
+            while (pos < end) {
+              int32_t u[kBatchN];
+#pragma unroll
+              for (int t = 0; t < kBatchN; t++) u[t] = pos + t < end ? __ldg(a.nbr + pos + t) : -1;
+#pragma unroll
+              for (int t = 0; t < kBatchN; t++)
+                if (u[t] >= 0) got |= ld_lane(a.fr + u[t]);
+              pos += kBatchN;
+              if (((got | vis) & all) == all) break;
+            }
+            nb = got & ~vis & all;
+            if (nb) {
+              a.visit[v] = vis | nb;
+              a.acc[v] = nb;
+            }
+          }
+        }
+        write_depths(a.depth, a.n, v, nb, level);
+        const unsigned fm = __ballot_sync(kFull, nb != 0);
+        if (fm) {
+          unsigned long long base = 0;
+          if (lane == 0) base = atomicAdd(touched, (unsigned long long)__popc(fm));
+          base = shfl(base, 0);
+          if (nb) a.tq[base + __popc(fm & ((1u << lane) - 1))] = (int32_t)v;
+        }
+      }
+    }
+    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+
+    // Clear the old frontier; reset the counters the next level fills.
+    for (int64_t i = tid; i < F; i += nthreads) a.fr[q[i]] = 0;
+    if (tid == 0) {
+      c->q_packed[cur ^ 1] = 0;
+      c->touched[(level + 1) & 1] = 0;
+    }
+    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+
+    // Install the new frontier from the vertices that received bits.
+    const int64_t T = (int64_t)__ldcg(touched);
+    for (int64_t i0 = warp << 5; i0 < T; i0 += nwarps << 5) {
+      const int64_t i = i0 + lane;
+      int32_t v = -1;
+      LaneT nb = 0;
+      if (i < T) {
+        v = a.tq[i];
+        nb = a.acc[v];
+        a.acc[v] = 0;
+        if (!bottom_up) {
+          const LaneT vis = a.visit[v];
+          nb &= ~vis;
+          if (nb) a.visit[v] = vis | nb;
+        }
+        if (nb) a.fr[v] = nb;
+      }
+      if (!bottom_up) {
+        // top-down claims come in queue order: depth writes one by one
+        LaneT x = nb;
+        while (x) {
+          const int b = (sizeof(LaneT) == 8) ? __ffsll((long long)x) - 1 : __ffs((int)x) - 1;
+          x &= x - 1;
+          a.depth[(int64_t)b * a.n + v] = (DepthT)level;
+        }
+      }
+      const bool keep = nb != 0;
+      const unsigned km = __ballot_sync(kFull, keep);
+      const unsigned long long deg = keep ? (unsigned long long)(a.off[v + 1] - a.off[v]) : 0;
+      const unsigned long long mine = keep ? (1ull << a.shift) + deg : 0;
+      const unsigned long long inc = warp_inclusive_sum(mine, lane);
+      unsigned long long base = 0;
+      if (km) {
+        if (lane == 31) base = atomicAdd(&c->q_packed[cur ^ 1], inc);
+        base = shfl(base, 31);
+        if (keep) qn[(base + inc - mine) >> a.shift] = v;
+      }
+    }
+    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+    cur ^= 1;
+    if (tid == 0) c->levels = level;
+  }
+  if (tid == 0) c->t_end = globaltimer();
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+namespace {
+
+#define ms_error (::gbbfs::last_error())
+
+template <typename OffT, typename LaneT, typename DepthT, int kB>
+const void* kernel_ptr() {
+  return (const void*)k_msbfs<OffT, LaneT, DepthT, kB>;
+}
+
+template <typename OffT, typename LaneT, typename DepthT>
+const void* pick_batch(int batch) {
+  switch (batch) {
+    case 4: return kernel_ptr<OffT, LaneT, DepthT, 4>();
+    case 16: return kernel_ptr<OffT, LaneT, DepthT, 16>();
+    default: return kernel_ptr<OffT, LaneT, DepthT, 8>();
+  }
+}
+
+template <typename OffT, typename LaneT>
+const void* pick_depth(int depth_bytes, int batch) {
+  return depth_bytes == 1 ? pick_batch<OffT, LaneT, uint8_t>(batch)
+                          : pick_batch<OffT, LaneT, int32_t>(batch);
+}
+
+template <typename OffT>
+const void* pick_kernel(const MsConfig& cfg, int depth_bytes) {
+  return cfg.lanes == 32 ? pick_depth<OffT, uint32_t>(depth_bytes, cfg.batch)
+                         : pick_depth<OffT, unsigned long long>(depth_bytes, cfg.batch);
+}
+
+const void* kernel_for(const gbbfs_graph* g, const MsConfig& cfg, int depth_bytes) {
+  return g->off32 ? pick_kernel<uint32_t>(cfg, depth_bytes)
+                  : pick_kernel<unsigned long long>(cfg, depth_bytes);
+}
+
+int ensure_state(gbbfs_graph* g, int depth_bytes) {
+  MsState* ms = g->ms;
+  if (ms && ms->depth_bytes == depth_bytes) return GBBFS_OK;
+  MsConfig keep;
+  if (ms) {
+    keep = ms->cfg;
+    msbfs_release(ms);
+    g->ms = nullptr;
+  }
+  const int64_t n = g->n;
+  // Lane words are allocated at 64 bits so both lane widths fit.
+  const size_t need = 3 * 8 * (size_t)n + 3 * 4 * (size_t)n +
+                      2 * (size_t)64 * n * depth_bytes + (16 << 20);
+  size_t free_b = 0, total_b = 0;
+  GB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (need > free_b) {
+    ms_error = "multi-source BFS needs " + std::to_string(need) + " bytes, " +
+               std::to_string(free_b) + " free";
+    return GBBFS_ERR_NOMEM;
+  }
+  ms = new MsState();
+  g->ms = ms;
+  ms->cfg = keep;
+  ms->n = n;
+  ms->depth_bytes = depth_bytes;
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 256));
+    if (e != cudaSuccess) {
+      ms_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+      return e == cudaErrorMemoryAllocation ? GBBFS_ERR_NOMEM : GBBFS_ERR_CUDA;
+    }
+    ms->bytes += (int64_t)bytes;
+    return GBBFS_OK;
+  };
+  GB_TRY(alloc(&ms->visit, 8 * (size_t)n));
+  GB_TRY(alloc(&ms->fr, 8 * (size_t)n));
+  GB_TRY(alloc(&ms->acc, 8 * (size_t)n));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
+  for (int i = 0; i < 2; i++) {
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->q[i]), 4 * (size_t)n));
+    GB_TRY(alloc(&ms->depth[i], (size_t)64 * n * depth_bytes));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), 64 * sizeof(int32_t)));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->ctl[i]), sizeof(MsCtl)));
+    GB_CUDA(cudaEventCreateWithFlags(&ms->computed[i], cudaEventDisableTiming));
+    GB_CUDA(cudaEventCreateWithFlags(&ms->copied[i], cudaEventDisableTiming));
+  }
+  GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_src), 2 * 64 * sizeof(int32_t),
+                        cudaHostAllocDefault));
+  GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_ctl), 2 * sizeof(MsCtl),
+                        cudaHostAllocDefault));
+  GB_CUDA(cudaStreamCreateWithFlags(&ms->copy_stream, cudaStreamNonBlocking));
+  GB_CUDA(cudaEventCreate(&ms->ev0));
+  GB_CUDA(cudaEventCreate(&ms->ev1));
+  // visit / fr / acc start (and are left) all-zero between batches: every
+  // batch clears them in its own graph before the kernel runs.
+  return GBBFS_OK;
+}
+
+template <typename OffT, typename LaneT, typename DepthT>
+int capture_batch(gbbfs_graph* g, int buf, int k) {
+  MsState* ms = g->ms;
+  const MsConfig& cfg = ms->cfg;
+  const void* fn = kernel_for(g, cfg, (int)sizeof(DepthT));
+  int per_sm = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
+  if (per_sm < 1) {
+    ms_error = "multi-source kernel does not fit on an SM";
+    return GBBFS_ERR_CUDA;
+  }
+  ms->grid = per_sm * g->sms;
+  MsArgs<OffT, LaneT, DepthT> a;
+  a.off = reinterpret_cast<const OffT*>(g->off);
+  a.nbr = g->nbr;
+  a.n = g->n;
+  a.m = g->m;
+  a.visit = reinterpret_cast<LaneT*>(ms->visit);
+  a.fr = reinterpret_cast<LaneT*>(ms->fr);
+  a.acc = reinterpret_cast<LaneT*>(ms->acc);
+  a.q0 = ms->q[0];
+  a.q1 = ms->q[1];
+  a.tq = ms->tq;
+  a.depth = reinterpret_cast<DepthT*>(ms->depth[buf]);
+  a.sources = ms->d_src[buf];
+  a.ctl = ms->ctl[buf];
+  a.k = k;
+  a.shift = g->shift;
+  a.alpha = std::max(1, cfg.alpha);
+  a.limit_ns = 5ull * 1000 * 1000 * 1000;  // 5 s per barrier
+
+  cudaStream_t s = g->stream;
+  const size_t lane_bytes = sizeof(LaneT) * (size_t)g->n;
+  GB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaMemcpyAsync(ms->d_src[buf], ms->h_src + 64 * buf, 64 * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->visit, 0, lane_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr, 0, lane_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->acc, 0, lane_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->ctl[buf], 0, sizeof(MsCtl), s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(ms->depth[buf], 0xff, (size_t)k * g->n * sizeof(DepthT), s);
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t lc;
+    memset(&lc, 0, sizeof lc);
+    lc.gridDim = dim3(ms->grid);
+    lc.blockDim = dim3(kThreads);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    void* args[] = {&a};
+    e = cudaLaunchKernelExC(&lc, fn, args);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ms->h_ctl + buf, ms->ctl[buf], sizeof(MsCtl), cudaMemcpyDeviceToHost, s);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) {
+    if (ms->exec[buf]) cudaGraphExecDestroy(ms->exec[buf]);
+    ms->exec[buf] = nullptr;
+    e = cudaGraphInstantiate(&ms->exec[buf], graph, 0);
+  }
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    ms_error = std::string("multi-source graph capture: ") + cudaGetErrorString(e);
+    return GBBFS_ERR_CUDA;
+  }
+  ms->exec_k[buf] = k;
+  ms->exec_cfg = cfg;
+  return GBBFS_OK;
+}
+
+template <typename OffT, typename LaneT>
+int capture_depth(gbbfs_graph* g, int buf, int k) {
+  return g->ms->depth_bytes == 1 ? capture_batch<OffT, LaneT, uint8_t>(g, buf, k)
+                                 : capture_batch<OffT, LaneT, int32_t>(g, buf, k);
+}
+
+template <typename OffT>
+int capture_lanes(gbbfs_graph* g, int buf, int k) {
+  return g->ms->cfg.lanes == 32 ? capture_depth<OffT, uint32_t>(g, buf, k)
+                                : capture_depth<OffT, unsigned long long>(g, buf, k);
+}
+
+bool same_cfg(const MsConfig& a, const MsConfig& b) {
+  return a.lanes == b.lanes && a.batch == b.batch && a.alpha == b.alpha;
+}
+
+// Launch one batch (k <= lanes sources) into depth buffer `buf`.
+int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
+  MsState* ms = g->ms;
+  for (int i = 0; i < k; i++) {
+    if (sources[i] < 0 || sources[i] >= g->n) {
+      ms_error = "source out of range";
+      return GBBFS_ERR_ARG;
+    }
+  }
+  // The buffer's previous results must have left the device first.
+  GB_CUDA(cudaStreamWaitEvent(g->stream, ms->copied[buf], 0));
+  if (!ms->exec[buf] || ms->exec_k[buf] != k || !same_cfg(ms->exec_cfg, ms->cfg)) {
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    int rc = g->off32 ? capture_lanes<uint32_t>(g, buf, k)
+                      : capture_lanes<unsigned long long>(g, buf, k);
+    if (rc != GBBFS_OK) return rc;
+  }
+  // The host copy of the sources is read by the graph's first node; wait
+  // until the previous launch that read this slot is done.
+  GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
+  memcpy(ms->h_src + 64 * buf, sources, sizeof(int32_t) * k);
+  GB_CUDA(cudaGraphLaunch(ms->exec[buf], g->stream));
+  GB_CUDA(cudaEventRecord(ms->computed[buf], g->stream));
+  return GBBFS_OK;
+}
+
+int check_batch(gbbfs_graph* g, int buf, int* levels) {
+  MsState* ms = g->ms;
+  GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
+  const MsCtl& c = ms->h_ctl[buf];
+  if (c.error) {
+    ms_error = c.error == GBBFS_ERR_TIMEOUT
+                   ? "multi-source grid barrier timed out"
+                   : "a depth exceeds the uint8 output range (use 4-byte depths)";
+    return c.error;
+  }
+  if (levels) *levels = std::max(*levels, c.levels);
+  return GBBFS_OK;
+}
+
+int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
+                void* host_out, gbbfs_ms_stats* st) {
+  if (!g || !sources || k <= 0 || (depth_bytes != 1 && depth_bytes != 4)) {
+    ms_error = "bad multi-source arguments";
+    return GBBFS_ERR_ARG;
+  }
+  GB_CUDA(cudaSetDevice(g->device));
+  GB_TRY(ensure_state(g, depth_bytes));
+  MsState* ms = g->ms;
+  const int lanes = ms->cfg.lanes;
+  const int64_t nb = (k + lanes - 1) / lanes;
+  if (!host_out && nb > 1) {
+    ms_error = "results left on the device hold one batch only";
+    return GBBFS_ERR_ARG;
+  }
+  const size_t per_src = (size_t)g->n * depth_bytes;
+  int levels = 0;
+  GB_CUDA(cudaEventRecord(ms->ev0, g->stream));
+  for (int64_t b = 0; b < nb; b++) {
+    const int buf = (int)(b & 1);
+    const int kb = (int)std::min<int64_t>(lanes, k - b * lanes);
+    GB_TRY(launch_batch(g, buf, sources + b * lanes, kb));
+    if (host_out) {
+      // Copy this batch out on the copy stream while the next one computes.
+      GB_CUDA(cudaStreamWaitEvent(ms->copy_stream, ms->computed[buf], 0));
+      GB_CUDA(cudaMemcpyAsync(static_cast<char*>(host_out) + (size_t)b * lanes * per_src,
+                              ms->depth[buf], (size_t)kb * per_src, cudaMemcpyDeviceToHost,
+                              ms->copy_stream));
+      GB_CUDA(cudaEventRecord(ms->copied[buf], ms->copy_stream));
+    }
+    if (b >= 1) GB_TRY(check_batch(g, buf ^ 1, &levels));
+    ms->last_buf = buf;
+    ms->last_k = kb;
+  }
+  GB_CUDA(cudaEventRecord(ms->ev1, g->stream));
+  GB_TRY(check_batch(g, ms->last_buf, &levels));
+  GB_CUDA(cudaStreamSynchronize(ms->copy_stream));
+  GB_CUDA(cudaStreamSynchronize(g->stream));
+  if (st) {
+    float ms_elapsed = 0;
+    GB_CUDA(cudaEventElapsedTime(&ms_elapsed, ms->ev0, ms->ev1));
+    st->device_ms = ms_elapsed;
+    st->batches = (int32_t)nb;
+    st->levels = levels;
+    st->lanes = lanes;
+    st->batch = ms->cfg.batch;
+    st->alpha = ms->cfg.alpha;
+  }
+  return GBBFS_OK;
+}
+
+}  // namespace
+}  // namespace gbbfs
+
+using namespace gbbfs;
+
+extern "C" {
+
+int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
+                void* depth_out, gbbfs_ms_stats* st) {
+  if (!depth_out) return GBBFS_ERR_ARG;
+  return run_batches(g, sources, k, depth_bytes, depth_out, st);
+}
+
+int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
+                       const void** depth_dev, gbbfs_ms_stats* st) {
+  if (!g) return GBBFS_ERR_ARG;
+  int rc = run_batches(g, sources, k, depth_bytes, nullptr, st);
+  if (rc != GBBFS_OK) return rc;
+  if (depth_dev) *depth_dev = g->ms->depth[g->ms->last_buf];
+  return GBBFS_OK;
+}
+
+int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg) {
+  if (!g || !cfg) return GBBFS_ERR_ARG;
+  if ((cfg->lanes != 32 && cfg->lanes != 64) ||
+      (cfg->batch != 4 && cfg->batch != 8 && cfg->batch != 16) || cfg->alpha < 1) {
+    last_error() = "lanes must be 32 or 64, batch 4, 8 or 16, alpha >= 1";
+    return GBBFS_ERR_ARG;
+  }
+  GB_CUDA(cudaSetDevice(g->device));
+  if (!g->ms) {
+    // keep the choice until the first batch allocates the state
+    GB_TRY(ensure_state(g, 1));
+  }
+  g->ms->cfg.lanes = cfg->lanes;
+  g->ms->cfg.batch = cfg->batch;
+  g->ms->cfg.alpha = cfg->alpha;
+  return GBBFS_OK;
+}
+
+int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg) {
+  if (!g || !cfg) return GBBFS_ERR_ARG;
+  MsConfig d;
+  const MsConfig& c = g->ms ? g->ms->cfg : d;
+  cfg->lanes = c.lanes;
+  cfg->batch = c.batch;
+  cfg->alpha = c.alpha;
+  return GBBFS_OK;
+}
+
+int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,
+                         gbbfs_ms_config* best) {
+  if (!g || !sample || k <= 0) return GBBFS_ERR_ARG;
+  static const int kLanes[] = {32, 64};
+  static const int kBatches[] = {4, 8, 16};
+  static const int kAlphas[] = {2, 6, 15, 40, 200};
+  double best_t = 1e300;
+  gbbfs_ms_config pick = {64, 8, 15};
+  for (int lanes : kLanes)
+    for (int batch : kBatches)
+      for (int alpha : kAlphas) {
+        gbbfs_ms_config c = {lanes, batch, alpha};
+        GB_TRY(gbbfs_msbfs_set_config(g, &c));
+        const int64_t kk = std::min<int64_t>(k, lanes);
+        gbbfs_ms_stats st;
+        GB_TRY(run_batches(g, sample, kk, depth_bytes, nullptr, &st));   // warm
+        GB_TRY(run_batches(g, sample, kk, depth_bytes, nullptr, &st));
+        const double per_query = st.device_ms / (double)kk;
+        if (per_query < best_t) {
+          best_t = per_query;
+          pick = c;
+        }
+      }
+  GB_TRY(gbbfs_msbfs_set_config(g, &pick));
+  if (best) *best = pick;
+  return GBBFS_OK;
+}
+
+}  // extern "C"

@@ -32,7 +32,8 @@ EXPORTS = (
     "gbbfs_bfs_device", "gbbfs_results", "gbbfs_result_device_ptrs", "gbbfs_strerror",
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
-    "gbbfs_append_bfs_output",
+    "gbbfs_append_bfs_output", "gbbfs_msbfs", "gbbfs_msbfs_device", "gbbfs_msbfs_set_config",
+    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune",
 )
 
 
@@ -61,6 +62,19 @@ class Stats(ctypes.Structure):
                 ("levels", ctypes.c_int32), ("device_ms", ctypes.c_double),
                 ("init_seconds", ctypes.c_double), ("reached", ctypes.c_int64),
                 ("alg_bytes", ctypes.c_int64)]
+
+
+class MsConfig(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int32), ("batch", ctypes.c_int32), ("alpha", ctypes.c_int32)]
+
+    def as_dict(self):
+        return dict(lanes=self.lanes, batch=self.batch, alpha=self.alpha)
+
+
+class MsStats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("batches", ctypes.c_int32),
+                ("levels", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("batch", ctypes.c_int32), ("alpha", ctypes.c_int32)]
 
 
 _lib = None
@@ -94,6 +108,11 @@ def lib():
             "gbbfs_write_sg": (I, [ctypes.c_char_p, P, P, i64, i64]),
             "gbbfs_pick_sources": (I, [P, i64, i64, I, P]),
             "gbbfs_append_bfs_output": (I, [ctypes.c_char_p, P, i64]),
+            "gbbfs_msbfs": (I, [P, P, i64, I, P, P]),
+            "gbbfs_msbfs_device": (I, [P, P, i64, I, PP, P]),
+            "gbbfs_msbfs_set_config": (I, [P, P]),
+            "gbbfs_msbfs_get_config": (I, [P, P]),
+            "gbbfs_msbfs_autotune": (I, [P, P, i64, I, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -312,3 +331,48 @@ def results(g, parent_out=None, depth_out=None):
 def write_bfs_output(path, parent):
     p = np.ascontiguousarray(parent, dtype=np.int32)
     _check(lib().gbbfs_append_bfs_output(os.fsencode(path), _p(p), len(p)), "append_bfs_output")
+
+
+# ---------------------------------------------------------------------------
+# Batched multi-source BFS.
+
+def msbfs(g, sources, depth_bytes=1, out=None, stats=False):
+    """Depths from many sources: array (k, n), uint8 (255 = unreached) or
+    int32 (-1 = unreached).  Row s equals DOBFS(g, sources[s]) depths."""
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    dt = np.uint8 if depth_bytes == 1 else np.int32
+    if out is None:
+        out = np.empty((len(src), g.n), dtype=dt)
+    st = MsStats()
+    _check(lib().gbbfs_msbfs(g.handle, _p(src), len(src), int(depth_bytes), _p(out),
+                             ctypes.byref(st)), "msbfs")
+    return (out, st) if stats else out
+
+
+def msbfs_device(g, sources, depth_bytes=1):
+    """One batch with results left in HBM; returns (device pointer, stats)."""
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    ptr = ctypes.c_void_p()
+    st = MsStats()
+    _check(lib().gbbfs_msbfs_device(g.handle, _p(src), len(src), int(depth_bytes),
+                                    ctypes.byref(ptr), ctypes.byref(st)), "msbfs_device")
+    return ptr.value, st
+
+
+def msbfs_set_config(g, lanes=64, batch=8, alpha=15):
+    c = MsConfig(lanes, batch, alpha)
+    _check(lib().gbbfs_msbfs_set_config(g.handle, ctypes.byref(c)), "msbfs_set_config")
+
+
+def msbfs_get_config(g):
+    c = MsConfig()
+    _check(lib().gbbfs_msbfs_get_config(g.handle, ctypes.byref(c)), "msbfs_get_config")
+    return c.as_dict()
+
+
+def msbfs_autotune(g, sample, depth_bytes=1):
+    src = np.ascontiguousarray(sample, dtype=np.int32)
+    c = MsConfig()
+    _check(lib().gbbfs_msbfs_autotune(g.handle, _p(src), len(src), int(depth_bytes),
+                                      ctypes.byref(c)), "msbfs_autotune")
+    return c.as_dict()

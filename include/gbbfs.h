@@ -113,6 +113,49 @@ int gbbfs_results(gbbfs_graph* g, int32_t* parent_out, int32_t* depth_out);
 int gbbfs_result_device_ptrs(gbbfs_graph* g, const int32_t** parent,
                              const int32_t** depth);
 
+/* ---- Batched multi-source BFS (no reference counterpart) ----
+ * Many sources of one graph at once, 32 or 64 per batch as a bitmask per
+ * vertex, in one persistent kernel per batch captured in a CUDA graph.  Its
+ * results are defined by the single-source search above: depth[s][v] equals
+ * the depth gbbfs_bfs (and the reference's DOBFS, src/bfs.cc:142-188) gives v
+ * from sources[s]. */
+typedef struct gbbfs_ms_config {
+  int32_t lanes;  /* sources per batch: 32 or 64                         */
+  int32_t batch;  /* neighbours one thread reads per bottom-up round: 4, 8, 16 */
+  int32_t alpha;  /* a level runs top-down while its frontier's summed degree
+                     is <= m_dir / alpha, bottom-up above                 */
+} gbbfs_ms_config;
+
+typedef struct gbbfs_ms_stats {
+  double device_ms;  /* device time of all batches                       */
+  int32_t batches;
+  int32_t levels;    /* deepest level of any batch                       */
+  int32_t lanes, batch, alpha;  /* configuration used                     */
+} gbbfs_ms_stats;
+
+/* BFS depths from k sources.  depth_out (host) receives k rows of n entries,
+ * row s for sources[s]: depth_bytes == 1 gives uint8 with 255 = unreached
+ * (GBBFS_ERR_ARG if a depth exceeds 254), depth_bytes == 4 gives int32 with
+ * -1 = unreached.  Batches run back to back; the copy of one batch overlaps
+ * the next batch's search (pinned depth_out makes the copy asynchronous). */
+int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
+                void* depth_out, gbbfs_ms_stats* st);
+
+/* One batch (k <= lanes) with the depths left in HBM; *depth_dev points at
+ * its k x n rows (valid until the next batched call on the handle). */
+int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
+                       const void** depth_dev, gbbfs_ms_stats* st);
+
+/* Choose or read the batched configuration. */
+int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg);
+int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg);
+
+/* Autotuner: time every configuration of the built-in grid (lanes x batch x
+ * alpha) on the given sample sources, keep the fastest per query on the
+ * handle and return it in *best. */
+int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,
+                         gbbfs_ms_config* best);
+
 /* Human-readable name of a status code. */
 const char* gbbfs_strerror(int status);
 

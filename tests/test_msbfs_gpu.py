@@ -1,0 +1,76 @@
+"""Batched multi-source BFS: every row must equal the single-source depths
+(which are pinned to the reference by test_bfs_gpu), bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def single_depths(native, g, sources):
+    return np.stack([native.DOBFS(g, int(s), depth=True)[1] for s in sources])
+
+
+def as_int32(d):
+    d = d.astype(np.int32)
+    d[d == 255] = -1
+    return d
+
+
+@pytest.mark.parametrize("lanes,batch,alpha", [(64, 8, 15), (32, 4, 2), (64, 16, 200),
+                                               (32, 8, 6), (64, 4, 1)])
+def test_msbfs_matches_single_source(native, lanes, batch, alpha):
+    off, nbr = native.make_graph(16, 16, False)
+    with native.Graph(off, nbr) as g:
+        srcs = native.pick_sources(off, 100)
+        ref = single_depths(native, g, srcs)
+        native.msbfs_set_config(g, lanes, batch, alpha)
+        assert native.msbfs_get_config(g) == dict(lanes=lanes, batch=batch, alpha=alpha)
+        d8, st = native.msbfs(g, srcs, 1, stats=True)
+        assert st.batches == (100 + lanes - 1) // lanes
+        assert np.array_equal(as_int32(d8), ref)
+        d32 = native.msbfs(g, srcs, 4)
+        assert np.array_equal(d32, ref)
+
+
+@pytest.mark.parametrize("scale,uniform", [(15, True), (18, False)])
+def test_msbfs_graphs(native, scale, uniform):
+    off, nbr = native.make_graph(scale, 16, uniform)
+    with native.Graph(off, nbr) as g:
+        srcs = native.pick_sources(off, 64)
+        ref = single_depths(native, g, srcs)
+        assert np.array_equal(native.msbfs(g, srcs, 4), ref)
+        # fewer sources than lanes, duplicate sources, any order
+        sub = np.array([srcs[3], srcs[3], srcs[0], srcs[7]], np.int32)
+        got = native.msbfs(g, sub, 4)
+        assert np.array_equal(got, ref[[3, 3, 0, 7]])
+
+
+def test_msbfs_handmade(native):
+    edges = np.array([[i, i + 1] for i in range(299)] +      # path: depth up to 299
+                     [[400 + i, 401 + i] for i in range(50)] + [[500, 501]], np.int32)
+    off, nbr = native.build_csr(edges, num_nodes=520)
+    with native.Graph(off, nbr) as g:
+        srcs = np.array([0, 150, 299, 400, 510, 425, 500], np.int32)   # 510 is isolated
+        ref = single_depths(native, g, srcs)
+        assert np.array_equal(native.msbfs(g, srcs, 4), ref)
+        # depths above 254 do not fit uint8: refused, not wrapped
+        with pytest.raises(native.GbbfsError) as e:
+            native.msbfs(g, srcs, 1)
+        assert e.value.status == native.ERR_ARG
+        ok = np.array([150, 400, 510], np.int32)
+        assert np.array_equal(as_int32(native.msbfs(g, ok, 1)), ref[[1, 3, 4]])
+
+
+def test_msbfs_device_and_autotune(native):
+    off, nbr = native.make_graph(17, 16, False)
+    with native.Graph(off, nbr) as g:
+        srcs = native.pick_sources(off, 64)
+        best = native.msbfs_autotune(g, srcs, 1)
+        assert best["lanes"] in (32, 64) and best["batch"] in (4, 8, 16)
+        assert native.msbfs_get_config(g) == best
+        ref = single_depths(native, g, srcs)
+        assert np.array_equal(as_int32(native.msbfs(g, srcs, 1)), ref)
+        ptr, st = native.msbfs_device(g, srcs[:best["lanes"]], 1)
+        assert ptr and st.batches == 1
+        with pytest.raises(native.GbbfsError):
+            native.msbfs_device(g, srcs[:10].tolist() + [len(off) + 5], 1)
