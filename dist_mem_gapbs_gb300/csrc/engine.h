@@ -69,4 +69,8 @@ struct gbbfs_graph {
   bool have_result = false;
   bool result_depth = false;
   gbbfs::MsState* ms = nullptr;
+  // Vertices whose adjacency the batched search cuts into work chunks, and
+  // the exclusive prefix of their chunk counts (filled at graph creation).
+  std::vector<int32_t> hubs;
+  std::vector<uint32_t> hub_chunk;
 };

@@ -5,27 +5,12 @@
 // single-source search (src/bfs.cc:142-188): depth[s][v] equals the depth that
 // a plain DOBFS from source s gives vertex v, bit for bit.
 //
-// Layout in HBM (n vertices, L = lane word, 32 or 64 bits):
-//   visit  L[n]   bit i set once source i has reached v
-//   fr     L[n]   bit i set if v is in the frontier of source i
-//   acc    L[n]   bits found for v in the level being expanded
-//   q0/q1  int32  vertices with fr != 0 (current / next), degree sums packed
-//   tq     int32  vertices that received bits in this level
-//   depth  D[k][n] per-source depth (uint8 with 255 = unreached, or int32
-//                 with -1), written directly in [source][vertex] order
-//
-// One persistent cooperative kernel runs all levels of a batch.  Per level it
-// picks a direction from the frontier's summed degree (top-down below
-// m / alpha, bottom-up above, alpha chosen by the autotuner):
-//   top-down: warp per frontier vertex, atomicOr of fr[u] & ~visit[v] into
-//             acc[v]; the first writer of a vertex queues it;
-//   bottom-up: thread per unfinished vertex, OR of fr[u] over its neighbours,
-//             stopping once every lane of v is found; depth written in place,
-//             coalesced per source.
-// Then the old frontier is cleared and the new one (acc) is installed.  Grid
-// barriers between the phases spin on a generation word with a time bound
-// (%globaltimer); a barrier that runs out sets an error word and every block
-// returns, so the host gets GBBFS_ERR_TIMEOUT instead of a hung GPU.
+// The kernel and the layout of its buffers are described in
+// msbfs_kernels.cuh.  This file owns the buffers, captures one CUDA graph per
+// batch buffer (sources copy, buffer resets, the persistent cooperative
+// kernel, a copy of the control block back to the host), runs batches back
+// to back with the copy of one batch's depths overlapping the next batch, and
+// holds the autotuner.  Depth rows are uint8 (255 = unreached) or int32 (-1).
 
 #include <cuda_runtime.h>
 
@@ -34,18 +19,9 @@
 #include <vector>
 
 #include "engine.h"
+#include "msbfs_kernels.cuh"
 
 namespace gbbfs {
-
-struct MsCtl {
-  unsigned long long q_packed[2];   // (count << shift) | summed degrees, per queue
-  unsigned long long touched[2];    // vertices queued in tq, per level parity
-  unsigned int bar_count;
-  unsigned int bar_gen;
-  int error;
-  int levels;
-  unsigned long long t_begin, t_end;
-};
 
 struct MsConfig {
   int lanes = 64;        // 32 or 64 sources per batch
@@ -60,8 +36,13 @@ struct MsState {
   void* visit = nullptr;
   void* fr = nullptr;
   void* acc = nullptr;
+  uint32_t* fbits = nullptr;
   int32_t* q[2] = {nullptr, nullptr};
+  uint32_t* qc[2] = {nullptr, nullptr};
   int32_t* tq = nullptr;
+  int32_t* hubs = nullptr;
+  uint32_t* hub_chunk = nullptr;
+  int64_t nhubs = 0;
   void* depth[2] = {nullptr, nullptr};
   int32_t* d_src[2] = {nullptr, nullptr};
   int32_t* h_src = nullptr;          // pinned, 2 x 64
@@ -86,6 +67,7 @@ void msbfs_release(MsState* ms) {
   for (int i = 0; i < 2; i++) {
     if (ms->exec[i]) cudaGraphExecDestroy(ms->exec[i]);
     cudaFree(ms->q[i]);
+    cudaFree(ms->qc[i]);
     cudaFree(ms->depth[i]);
     cudaFree(ms->d_src[i]);
     cudaFree(ms->ctl[i]);
@@ -95,273 +77,16 @@ void msbfs_release(MsState* ms) {
   cudaFree(ms->visit);
   cudaFree(ms->fr);
   cudaFree(ms->acc);
+  cudaFree(ms->fbits);
   cudaFree(ms->tq);
+  cudaFree(ms->hubs);
+  cudaFree(ms->hub_chunk);
   if (ms->h_src) cudaFreeHost(ms->h_src);
   if (ms->h_ctl) cudaFreeHost(ms->h_ctl);
   if (ms->ev0) cudaEventDestroy(ms->ev0);
   if (ms->ev1) cudaEventDestroy(ms->ev1);
   if (ms->copy_stream) cudaStreamDestroy(ms->copy_stream);
   delete ms;
-}
-
-// ---------------------------------------------------------------------------
-// Device side.
-
-template <typename LaneT>
-__device__ __forceinline__ LaneT atomic_or_lane(LaneT* p, LaneT v) {
-  if constexpr (sizeof(LaneT) == 8)
-    return (LaneT)atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
-  else
-    return (LaneT)atomicOr(reinterpret_cast<unsigned int*>(p), (unsigned int)v);
-}
-
-template <typename LaneT>
-__device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
-  if constexpr (sizeof(LaneT) == 8)
-    return (LaneT)__ldcg(reinterpret_cast<const unsigned long long*>(p));
-  else
-    return (LaneT)__ldcg(reinterpret_cast<const unsigned int*>(p));
-}
-
-template <typename LaneT>
-__device__ __forceinline__ LaneT warp_or(LaneT x) {
-#pragma unroll
-  for (int o = 16; o; o >>= 1) x |= shfl(x, (int)(threadIdx.x & 31) ^ o);
-  return x;
-}
-
-// Grid-wide barrier with a time bound.  Returns false (and every later call
-// returns false at once) when any block has given up.
-__device__ __forceinline__ bool grid_barrier(MsCtl* c, unsigned nblocks,
-                                             unsigned long long limit_ns) {
-  __syncthreads();
-  __shared__ int ok;
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile unsigned* vgen = &c->bar_gen;
-    const unsigned gen = *vgen;
-    __threadfence();
-    if (atomicAdd(&c->bar_count, 1u) == nblocks - 1) {
-      c->bar_count = 0;
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
-    } else {
-      const unsigned long long t0 = globaltimer();
-      while (*vgen == gen) {
-        if (*(volatile int*)&c->error) {
-          ok = 0;
-          break;
-        }
-        if (globaltimer() - t0 > limit_ns) {
-          atomicExch(&c->error, GBBFS_ERR_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    if (*(volatile int*)&c->error) ok = 0;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
-template <typename OffT, typename LaneT, typename DepthT>
-struct MsArgs {
-  const OffT* off;
-  const int32_t* nbr;
-  int64_t n, m;
-  LaneT* visit;
-  LaneT* fr;
-  LaneT* acc;
-  int32_t* q0;
-  int32_t* q1;
-  int32_t* tq;
-  DepthT* depth;
-  const int32_t* sources;
-  MsCtl* ctl;
-  int k;
-  int shift;
-  int alpha;
-  unsigned long long limit_ns;
-};
-
-// Write depth `level` for every source bit of `nb` at vertex v.  Called by a
-// whole warp; lanes with consecutive v write consecutive bytes per source.
-template <typename LaneT, typename DepthT>
-__device__ __forceinline__ void write_depths(DepthT* depth, int64_t n, int64_t v, LaneT nb,
-                                             int level) {
-  LaneT any = warp_or(nb);
-  while (any) {
-    const int i = (sizeof(LaneT) == 8) ? __ffsll((long long)any) - 1 : __ffs((int)any) - 1;
-    any &= any - 1;
-    if ((nb >> i) & 1) depth[(int64_t)i * n + v] = (DepthT)level;
-  }
-}
-
-template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
-__global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
-  MsCtl* c = a.ctl;
-  const unsigned nblocks = gridDim.x;
-  const int lane = threadIdx.x & 31;
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  const int64_t warp = tid >> 5;
-  const int64_t nwarps = nthreads >> 5;
-  const unsigned long long emask = (1ull << a.shift) - 1;
-  const LaneT all = a.k >= (int)(8 * sizeof(LaneT)) ? (LaneT)~(LaneT)0
-                                                     : (LaneT)(((LaneT)1 << a.k) - 1);
-  const int max_level = sizeof(DepthT) == 1 ? 254 : 0x7ffffffe;
-  if (tid == 0) c->t_begin = globaltimer();
-
-  // Sources: lane i starts at sources[i] (depth 0).  A vertex that is the
-  // source of several lanes is queued once.
-  if (blockIdx.x == 0 && threadIdx.x < a.k) {
-    const int i = threadIdx.x;
-    const int32_t s = a.sources[i];
-    const LaneT bit = (LaneT)1 << i;
-    atomic_or_lane(a.visit + s, bit);
-    a.depth[(int64_t)i * a.n + s] = 0;
-    if (atomic_or_lane(a.fr + s, bit) == 0) {
-      const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
-      const unsigned long long at =
-          atomicAdd(&c->q_packed[0], (1ull << a.shift) + deg) >> a.shift;
-      a.q0[at] = s;
-    }
-  }
-  if (!grid_barrier(c, nblocks, a.limit_ns)) return;
-
-  int cur = 0;
-  for (int level = 1;; level++) {
-    const unsigned long long p = __ldcg(&c->q_packed[cur]);
-    const int64_t F = (int64_t)(p >> a.shift);
-    const uint64_t E = p & emask;
-    if (F == 0) break;
-    if (level > max_level) {
-      if (tid == 0) atomicExch(&c->error, GBBFS_ERR_ARG);
-      break;
-    }
-    const int32_t* q = cur ? a.q1 : a.q0;
-    int32_t* qn = cur ? a.q0 : a.q1;
-    unsigned long long* touched = &c->touched[level & 1];
-    const bool bottom_up = E > (uint64_t)(a.m / a.alpha);
-
-    if (!bottom_up) {
-      // Top-down: warp per frontier vertex.
-      for (int64_t i = warp; i < F; i += nwarps) {
-        const int32_t u = q[i];
-        const LaneT f = ld_lane(a.fr + u);
-        const uint64_t b0 = (uint64_t)a.off[u], b1 = (uint64_t)a.off[u + 1];
-        for (uint64_t e0 = b0; e0 < b1; e0 += 32) {
-          const uint64_t e = e0 + lane;
-          bool first = false;
-          int32_t v = 0;
-          if (e < b1) {
-            v = __ldg(a.nbr + e);
-            const LaneT nb = f & ~ld_lane(a.visit + v);
-            if (nb) first = atomic_or_lane(a.acc + v, nb) == 0;
-          }
-          const unsigned fm = __ballot_sync(kFull, first);
-          if (fm) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(touched, (unsigned long long)__popc(fm));
-            base = shfl(base, 0);
-            if (first) a.tq[base + __popc(fm & ((1u << lane) - 1))] = v;
-          }
-        }
-      }
-    } else {
-      // Bottom-up: thread per vertex, all lanes of v at once.
-      for (int64_t v0 = warp << 5; v0 < a.n; v0 += nwarps << 5) {
-        const int64_t v = v0 + lane;
-        LaneT nb = 0;
-        if (v < a.n) {
-          const LaneT vis = ld_lane(a.visit + v);
-          if (vis != all) {
-            uint64_t pos = (uint64_t)a.off[v];
-            const uint64_t end = (uint64_t)a.off[v + 1];
-            LaneT got = 0;
-            while (pos < end) {
-              int32_t u[kBatchN];
-#pragma unroll
-              for (int t = 0; t < kBatchN; t++) u[t] = pos + t < end ? __ldg(a.nbr + pos + t) : -1;
-#pragma unroll
-              for (int t = 0; t < kBatchN; t++)
-                if (u[t] >= 0) got |= ld_lane(a.fr + u[t]);
-              pos += kBatchN;
-              if (((got | vis) & all) == all) break;
-            }
-            nb = got & ~vis & all;
-            if (nb) {
-              a.visit[v] = vis | nb;
-              a.acc[v] = nb;
-            }
-          }
-        }
-        write_depths(a.depth, a.n, v, nb, level);
-        const unsigned fm = __ballot_sync(kFull, nb != 0);
-        if (fm) {
-          unsigned long long base = 0;
-          if (lane == 0) base = atomicAdd(touched, (unsigned long long)__popc(fm));
-          base = shfl(base, 0);
-          if (nb) a.tq[base + __popc(fm & ((1u << lane) - 1))] = (int32_t)v;
-        }
-      }
-    }
-    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
-
-    // Clear the old frontier; reset the counters the next level fills.
-    for (int64_t i = tid; i < F; i += nthreads) a.fr[q[i]] = 0;
-    if (tid == 0) {
-      c->q_packed[cur ^ 1] = 0;
-      c->touched[(level + 1) & 1] = 0;
-    }
-    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
-
-    // Install the new frontier from the vertices that received bits.
-    const int64_t T = (int64_t)__ldcg(touched);
-    for (int64_t i0 = warp << 5; i0 < T; i0 += nwarps << 5) {
-      const int64_t i = i0 + lane;
-      int32_t v = -1;
-      LaneT nb = 0;
-      if (i < T) {
-        v = a.tq[i];
-        nb = a.acc[v];
-        a.acc[v] = 0;
-        if (!bottom_up) {
-          const LaneT vis = a.visit[v];
-          nb &= ~vis;
-          if (nb) a.visit[v] = vis | nb;
-        }
-        if (nb) a.fr[v] = nb;
-      }
-      if (!bottom_up) {
-        // top-down claims come in queue order: depth writes one by one
-        LaneT x = nb;
-        while (x) {
-          const int b = (sizeof(LaneT) == 8) ? __ffsll((long long)x) - 1 : __ffs((int)x) - 1;
-          x &= x - 1;
-          a.depth[(int64_t)b * a.n + v] = (DepthT)level;
-        }
-      }
-      const bool keep = nb != 0;
-      const unsigned km = __ballot_sync(kFull, keep);
-      const unsigned long long deg = keep ? (unsigned long long)(a.off[v + 1] - a.off[v]) : 0;
-      const unsigned long long mine = keep ? (1ull << a.shift) + deg : 0;
-      const unsigned long long inc = warp_inclusive_sum(mine, lane);
-      unsigned long long base = 0;
-      if (km) {
-        if (lane == 31) base = atomicAdd(&c->q_packed[cur ^ 1], inc);
-        base = shfl(base, 31);
-        if (keep) qn[(base + inc - mine) >> a.shift] = v;
-      }
-    }
-    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
-    cur ^= 1;
-    if (tid == 0) c->levels = level;
-  }
-  if (tid == 0) c->t_end = globaltimer();
 }
 
 // ---------------------------------------------------------------------------
@@ -439,9 +164,21 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   GB_TRY(alloc(&ms->visit, 8 * (size_t)n));
   GB_TRY(alloc(&ms->fr, 8 * (size_t)n));
   GB_TRY(alloc(&ms->acc, 8 * (size_t)n));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
+  // Hubs (degree above kMsHubDeg) and the prefix of their work chunks.
+  ms->nhubs = (int64_t)g->hubs.size();
+  if (ms->nhubs) {
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->hubs), 4 * (size_t)ms->nhubs));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->hub_chunk), 4 * (size_t)(ms->nhubs + 1)));
+    GB_CUDA(cudaMemcpy(ms->hubs, g->hubs.data(), 4 * (size_t)ms->nhubs,
+                       cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(ms->hub_chunk, g->hub_chunk.data(), 4 * (size_t)(ms->nhubs + 1),
+                       cudaMemcpyHostToDevice));
+  }
   for (int i = 0; i < 2; i++) {
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->q[i]), 4 * (size_t)n));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->qc[i]), 4 * (size_t)n));
     GB_TRY(alloc(&ms->depth[i], (size_t)64 * n * depth_bytes));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), 64 * sizeof(int32_t)));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->ctl[i]), sizeof(MsCtl)));
@@ -480,9 +217,16 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.visit = reinterpret_cast<LaneT*>(ms->visit);
   a.fr = reinterpret_cast<LaneT*>(ms->fr);
   a.acc = reinterpret_cast<LaneT*>(ms->acc);
+  a.W = g->W;
+  a.fbits = ms->fbits;
   a.q0 = ms->q[0];
   a.q1 = ms->q[1];
+  a.qc0 = ms->qc[0];
+  a.qc1 = ms->qc[1];
   a.tq = ms->tq;
+  a.hubs = ms->hubs;
+  a.hub_chunk = ms->hub_chunk;
+  a.nhubs = ms->nhubs;
   a.depth = reinterpret_cast<DepthT*>(ms->depth[buf]);
   a.sources = ms->d_src[buf];
   a.ctl = ms->ctl[buf];
@@ -499,6 +243,7 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->visit, 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr, 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->acc, 0, lane_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->fbits, 0, 4 * (size_t)g->W, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->ctl[buf], 0, sizeof(MsCtl), s);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(ms->depth[buf], 0xff, (size_t)k * g->n * sizeof(DepthT), s);

@@ -1,0 +1,408 @@
+// Device side of the batched multi-source BFS (sm_103a).
+//
+// Layout in HBM (n vertices, W = ceil(n/32), L = lane word of 32 or 64 bits):
+//   visit  L[n]      bit i set once source i has reached v
+//   fr     L[n]      bit i set if v is in the frontier of source i
+//   acc    L[n]      bits found for v in the level being expanded
+//   fbits  u32[W]    union of all frontiers (v has fr[v] != 0): tested before
+//                    fr[v] is read, so neighbours outside every frontier cost
+//                    one L2-resident bit instead of a lane word
+//   q0/q1  int32     frontier vertices (current / next) and qc0/qc1, the
+//                    first top-down work chunk of each entry
+//   tq     int32     vertices that received bits in this level
+//   hubs   int32     vertices of degree > kMsHubDeg with their chunk prefix
+//   depth  D[k][n]   per-source depth, [source][vertex] order
+//
+// One persistent cooperative kernel runs all levels of a batch.  Per level:
+//   expand   top-down (frontier summed degree <= m / alpha): work items of
+//            kMsTdChunk edges of one frontier vertex, a warp per item,
+//            atomicOr of fr[u] & ~visit[v] into acc[v];
+//            bottom-up: a warp per 32 consecutive vertices — thread per vertex
+//            up to kMsLight neighbours, the whole warp per vertex up to
+//            kMsHubDeg, early exit once every lane of v is found — plus the
+//            adjacency of hubs cut into kMsHubChunk-edge items merged into
+//            acc by atomicOr;
+//   clear    the old frontier (fr, fbits);
+//   install  the new frontier from acc, queued with its work-chunk prefix.
+// Grid barriers between the phases spin on a generation word with a time
+// bound; a barrier that runs out sets an error word and every block returns.
+#pragma once
+
+#include "bfs_common.cuh"
+
+namespace gbbfs {
+
+constexpr int kMsLight = 32;
+constexpr int kMsHubDeg = 2048;
+constexpr int kMsHubChunk = 2048;
+constexpr int kMsTdChunk = 1024;
+
+struct MsCtl {
+  unsigned long long q_packed[2];   // (count << shift) | top-down chunks, per queue
+  unsigned long long q_edges[2];    // summed degrees of each queue
+  unsigned long long touched[2];    // vertices queued in tq, per level parity
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int error;
+  int levels;
+  unsigned long long t_begin, t_end;
+};
+
+template <typename OffT, typename LaneT, typename DepthT>
+struct MsArgs {
+  const OffT* off;
+  const int32_t* nbr;
+  int64_t n, m, W;
+  LaneT* visit;
+  LaneT* fr;
+  LaneT* acc;
+  uint32_t* fbits;
+  int32_t* q0;
+  int32_t* q1;
+  uint32_t* qc0;
+  uint32_t* qc1;
+  int32_t* tq;
+  const int32_t* hubs;
+  const uint32_t* hub_chunk;   // nhubs + 1 entries
+  int64_t nhubs;
+  DepthT* depth;
+  const int32_t* sources;
+  MsCtl* ctl;
+  int k;
+  int shift;
+  int alpha;
+  unsigned long long limit_ns;
+};
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT atomic_or_lane(LaneT* p, LaneT v) {
+  if constexpr (sizeof(LaneT) == 8)
+    return (LaneT)atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+  else
+    return (LaneT)atomicOr(reinterpret_cast<unsigned int*>(p), (unsigned int)v);
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
+  if constexpr (sizeof(LaneT) == 8)
+    return (LaneT)__ldcg(reinterpret_cast<const unsigned long long*>(p));
+  else
+    return (LaneT)__ldcg(reinterpret_cast<const unsigned int*>(p));
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT warp_or(LaneT x) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x |= shfl(x, (int)(threadIdx.x & 31) ^ o);
+  return x;
+}
+
+template <typename LaneT>
+__device__ __forceinline__ int lowest_bit(LaneT x) {
+  if constexpr (sizeof(LaneT) == 8)
+    return __ffsll((long long)x) - 1;
+  else
+    return __ffs((int)x) - 1;
+}
+
+__device__ __forceinline__ bool in_frontier(const uint32_t* fbits, int32_t u) {
+  return (__ldcg(fbits + (u >> 5)) >> (u & 31)) & 1u;
+}
+
+// Grid-wide barrier with a time bound.  Returns false (and every later call
+// returns false at once) when any block has given up.
+__device__ __forceinline__ bool grid_barrier(MsCtl* c, unsigned nblocks,
+                                             unsigned long long limit_ns) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned* vgen = &c->bar_gen;
+    const unsigned gen = *vgen;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == nblocks - 1) {
+      c->bar_count = 0;
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer();
+      while (*vgen == gen) {
+        if (*(volatile int*)&c->error) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer() - t0 > limit_ns) {
+          atomicExch(&c->error, GBBFS_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)&c->error) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Depth `level` for every source bit of `nb` at vertex v.  Called by a whole
+// warp; lanes with consecutive v write consecutive entries of each row.
+template <typename LaneT, typename DepthT>
+__device__ __forceinline__ void write_depths(DepthT* depth, int64_t n, int64_t v, LaneT nb,
+                                             int level) {
+  LaneT any = warp_or(nb);
+  while (any) {
+    const int i = lowest_bit(any);
+    any &= any - 1;
+    if ((nb >> i) & 1) depth[(int64_t)i * n + v] = (DepthT)level;
+  }
+}
+
+// Append the lanes with `keep` to a vertex list (one atomic per warp).
+__device__ __forceinline__ void warp_append(unsigned long long* counter, int32_t* list,
+                                            bool keep, int32_t v) {
+  const int lane = threadIdx.x & 31;
+  const unsigned km = __ballot_sync(kFull, keep);
+  if (km) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, (unsigned long long)__popc(km));
+    base = shfl(base, 0);
+    if (keep) list[base + __popc(km & ((1u << lane) - 1))] = v;
+  }
+}
+
+template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
+__global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
+  MsCtl* c = a.ctl;
+  const unsigned nblocks = gridDim.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int64_t warp = tid >> 5;
+  const int64_t nwarps = nthreads >> 5;
+  const unsigned long long emask = (1ull << a.shift) - 1;
+  const LaneT all = a.k >= (int)(8 * sizeof(LaneT)) ? (LaneT)~(LaneT)0
+                                                     : (LaneT)(((LaneT)1 << a.k) - 1);
+  const int max_level = sizeof(DepthT) == 1 ? 254 : 0x7ffffffe;
+  const int64_t hub_chunks = a.nhubs ? (int64_t)a.hub_chunk[a.nhubs] : 0;
+  if (tid == 0) c->t_begin = globaltimer();
+
+  // Sources: lane i starts at sources[i] with depth 0.  A vertex that is the
+  // source of several lanes is queued once.
+  if (blockIdx.x == 0 && threadIdx.x < a.k) {
+    const int i = threadIdx.x;
+    const int32_t s = a.sources[i];
+    const LaneT bit = (LaneT)1 << i;
+    atomic_or_lane(a.visit + s, bit);
+    a.depth[(int64_t)i * a.n + s] = 0;
+    if (atomic_or_lane(a.fr + s, bit) == 0) {
+      const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
+      const unsigned long long chunks = (deg + kMsTdChunk - 1) / kMsTdChunk;
+      const unsigned long long at = atomicAdd(&c->q_packed[0], (1ull << a.shift) + chunks);
+      a.q0[at >> a.shift] = s;
+      a.qc0[at >> a.shift] = (uint32_t)(at & emask);
+      atomicAdd(&c->q_edges[0], deg);
+      atomicOr(a.fbits + (s >> 5), 1u << (s & 31));
+    }
+  }
+  if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+
+  int cur = 0;
+  for (int level = 1;; level++) {
+    const unsigned long long p = __ldcg(&c->q_packed[cur]);
+    const int64_t F = (int64_t)(p >> a.shift);
+    const int64_t C = (int64_t)(p & emask);
+    const unsigned long long E = __ldcg(&c->q_edges[cur]);
+    if (F == 0) break;
+    if (level > max_level) {
+      if (tid == 0) atomicExch(&c->error, GBBFS_ERR_ARG);
+      break;
+    }
+    const int32_t* q = cur ? a.q1 : a.q0;
+    const uint32_t* qc = cur ? a.qc1 : a.qc0;
+    int32_t* qn = cur ? a.q0 : a.q1;
+    uint32_t* qcn = cur ? a.qc0 : a.qc1;
+    unsigned long long* touched = &c->touched[level & 1];
+    const bool bottom_up = E > (unsigned long long)(a.m / a.alpha);
+
+    if (!bottom_up) {
+      // Top-down: a warp per work chunk of one frontier vertex.
+      for (int64_t ch = warp; ch < C; ch += nwarps) {
+        int64_t lo = 0, hi = F - 1;
+        while (lo < hi) {
+          const int64_t mid = (lo + hi + 1) >> 1;
+          if ((int64_t)qc[mid] <= ch) lo = mid; else hi = mid - 1;
+        }
+        const int32_t u = q[lo];
+        const LaneT f = ld_lane(a.fr + u);
+        const uint64_t b = (uint64_t)a.off[u] + (uint64_t)(ch - qc[lo]) * kMsTdChunk;
+        const uint64_t ue = (uint64_t)a.off[u + 1];
+        const uint64_t e = b + kMsTdChunk < ue ? b + kMsTdChunk : ue;
+        for (uint64_t e0 = b; e0 < e; e0 += 32) {
+          bool first = false;
+          int32_t v = 0;
+          if (e0 + lane < e) {
+            v = __ldg(a.nbr + e0 + lane);
+            const LaneT nb = f & ~ld_lane(a.visit + v);
+            if (nb) first = atomic_or_lane(a.acc + v, nb) == 0;
+          }
+          warp_append(touched, a.tq, first, v);
+        }
+      }
+    } else {
+      // Bottom-up over tiles of 32 consecutive vertices.
+      for (int64_t v0 = warp << 5; v0 < a.n; v0 += nwarps << 5) {
+        const int64_t v = v0 + lane;
+        LaneT vis = all;
+        uint64_t b = 0, e = 0;
+        if (v < a.n) {
+          vis = ld_lane(a.visit + v);
+          b = (uint64_t)a.off[v];
+          e = (uint64_t)a.off[v + 1];
+        }
+        const bool need = ((vis & all) != all) && e > b;
+        const uint64_t deg = e - b;
+        LaneT nb = 0;
+        if (need && deg <= kMsLight) {
+          LaneT got = 0;
+          for (uint64_t pos = b; pos < e; pos += kBatchN) {
+            int32_t u[kBatchN];
+#pragma unroll
+            for (int t = 0; t < kBatchN; t++) u[t] = pos + t < e ? __ldg(a.nbr + pos + t) : -1;
+            bool in[kBatchN];
+#pragma unroll
+            for (int t = 0; t < kBatchN; t++) in[t] = u[t] >= 0 && in_frontier(a.fbits, u[t]);
+#pragma unroll
+            for (int t = 0; t < kBatchN; t++)
+              if (in[t]) got |= ld_lane(a.fr + u[t]);
+            if (((got | vis) & all) == all) break;
+          }
+          nb = got & ~vis & all;
+        }
+        unsigned mids = __ballot_sync(kFull, need && deg > kMsLight && deg <= kMsHubDeg);
+        while (mids) {
+          const int t = __ffs(mids) - 1;
+          mids &= mids - 1;
+          const LaneT vt = shfl(vis, t);
+          const uint64_t bt = shfl(b, t), et = shfl(e, t);
+          LaneT got = 0;
+          for (uint64_t e0 = bt; e0 < et; e0 += 32) {
+            LaneT x = 0;
+            if (e0 + lane < et) {
+              const int32_t u = __ldg(a.nbr + e0 + lane);
+              if (in_frontier(a.fbits, u)) x = ld_lane(a.fr + u);
+            }
+            got |= warp_or(x);
+            if (((got | vt) & all) == all) break;
+          }
+          if (lane == t) nb = got & ~vt & all;
+        }
+        if (nb) {
+          a.visit[v] = vis | nb;
+          a.acc[v] = nb;
+        }
+        write_depths(a.depth, a.n, v, nb, level);
+        warp_append(touched, a.tq, nb != 0, (int32_t)v);
+      }
+      // Hubs: their adjacency cut into work items, merged by atomicOr.
+      for (int64_t hc = warp; hc < hub_chunks; hc += nwarps) {
+        int64_t lo = 0, hi = a.nhubs - 1;
+        while (lo < hi) {
+          const int64_t mid = (lo + hi + 1) >> 1;
+          if ((int64_t)a.hub_chunk[mid] <= hc) lo = mid; else hi = mid - 1;
+        }
+        const int32_t v = a.hubs[lo];
+        const LaneT vis = ld_lane(a.visit + v);
+        if ((vis & all) == all) continue;
+        const uint64_t b = (uint64_t)a.off[v] + (uint64_t)(hc - a.hub_chunk[lo]) * kMsHubChunk;
+        const uint64_t ve = (uint64_t)a.off[v + 1];
+        const uint64_t e = b + kMsHubChunk < ve ? b + kMsHubChunk : ve;
+        LaneT got = 0;
+        for (uint64_t e0 = b; e0 < e; e0 += 32) {
+          LaneT x = 0;
+          if (e0 + lane < e) {
+            const int32_t u = __ldg(a.nbr + e0 + lane);
+            if (in_frontier(a.fbits, u)) x = ld_lane(a.fr + u);
+          }
+          got |= warp_or(x);
+          if (((got | vis) & all) == all) break;
+        }
+        const LaneT part = got & ~vis & all;
+        bool first = false;
+        if (lane == 0 && part) first = atomic_or_lane(a.acc + v, part) == 0;
+        warp_append(touched, a.tq, first, v);
+      }
+    }
+    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+
+    // Clear the old frontier; reset the counters the next level fills.
+    for (int64_t i = tid; i < F; i += nthreads) {
+      const int32_t u = q[i];
+      a.fr[u] = 0;
+      atomicAnd(a.fbits + (u >> 5), ~(1u << (u & 31)));
+    }
+    if (tid == 0) {
+      c->q_packed[cur ^ 1] = 0;
+      c->q_edges[cur ^ 1] = 0;
+      c->touched[(level + 1) & 1] = 0;
+    }
+    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+
+    // Install the new frontier from the vertices that received bits.
+    const int64_t T = (int64_t)__ldcg(touched);
+    for (int64_t i0 = warp << 5; i0 < T; i0 += nwarps << 5) {
+      const int64_t i = i0 + lane;
+      int32_t v = -1;
+      LaneT nb = 0;
+      unsigned long long deg = 0;
+      if (i < T) {
+        v = a.tq[i];
+        deg = (unsigned long long)(a.off[v + 1] - a.off[v]);
+        nb = a.acc[v];
+        a.acc[v] = 0;
+        if (!bottom_up || deg > (unsigned long long)kMsHubDeg) {
+          // merged by atomics: mask and record here
+          const LaneT vis = a.visit[v];
+          nb &= ~vis;
+          if (nb) {
+            a.visit[v] = vis | nb;
+            for (LaneT x = nb; x; x &= x - 1)
+              a.depth[(int64_t)lowest_bit(x) * a.n + v] = (DepthT)level;
+          }
+        }
+        if (nb) {
+          a.fr[v] = nb;
+          atomicOr(a.fbits + (v >> 5), 1u << (v & 31));
+        }
+      }
+      const bool keep = nb != 0;
+      const unsigned km = __ballot_sync(kFull, keep);
+      if (km) {
+        const unsigned long long chunks = keep ? (deg + kMsTdChunk - 1) / kMsTdChunk : 0;
+        const unsigned long long mine = keep ? (1ull << a.shift) + chunks : 0;
+        const unsigned long long inc = warp_inclusive_sum(mine, lane);
+        unsigned long long dsum = keep ? deg : 0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) dsum += __shfl_xor_sync(kFull, dsum, o);
+        unsigned long long base = 0;
+        if (lane == 31) {
+          base = atomicAdd(&c->q_packed[cur ^ 1], inc);
+          atomicAdd(&c->q_edges[cur ^ 1], dsum);
+        }
+        base = shfl(base, 31);
+        if (keep) {
+          const unsigned long long at = base + inc - mine;
+          qn[at >> a.shift] = v;
+          qcn[at >> a.shift] = (uint32_t)(at & emask);
+        }
+      }
+    }
+    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+    cur ^= 1;
+    if (tid == 0) c->levels = level;
+  }
+  if (tid == 0) c->t_end = globaltimer();
+}
+
+}  // namespace gbbfs

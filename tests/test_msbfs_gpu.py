@@ -61,6 +61,24 @@ def test_msbfs_handmade(native):
         assert np.array_equal(as_int32(native.msbfs(g, ok, 1)), ref[[1, 3, 4]])
 
 
+@pytest.mark.parametrize("alpha", [1, 15, 100000])
+def test_msbfs_hubs(native, alpha):
+    """Vertices above the hub degree are cut into work chunks in both directions."""
+    rng = np.random.default_rng(3)
+    edges = np.concatenate([
+        np.stack([np.zeros(9000, np.int32), np.arange(1, 9001, dtype=np.int32)], 1),
+        np.stack([np.full(5000, 9001, np.int32), rng.integers(0, 20000, 5000)], 1),
+        rng.integers(0, 20000, size=(30000, 2))]).astype(np.int32)
+    off, nbr = native.build_csr(edges)
+    with native.Graph(off, nbr) as g:
+        deg = np.diff(off)
+        srcs = np.array([0, 9001, int(np.argmax(deg[1:]) + 1)] +
+                        list(native.pick_sources(off, 40)), np.int32)
+        ref = single_depths(native, g, srcs)
+        native.msbfs_set_config(g, 64, 8, alpha)
+        assert np.array_equal(native.msbfs(g, srcs, 4), ref)
+
+
 def test_msbfs_device_and_autotune(native):
     off, nbr = native.make_graph(17, 16, False)
     with native.Graph(off, nbr) as g:
