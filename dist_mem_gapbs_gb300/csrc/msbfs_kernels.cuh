@@ -172,6 +172,34 @@ __device__ __forceinline__ void warp_append(unsigned long long* counter, int32_t
   }
 }
 
+// OR of fr[u] over the neighbours nbr[b..e) of one vertex, by the whole warp:
+// 4 x 32 neighbours per round, every load of a round issued before any is
+// used, early exit once (result | vis) covers every lane.
+template <typename OffT, typename LaneT, typename DepthT>
+__device__ __forceinline__ LaneT warp_gather_or(const MsArgs<OffT, LaneT, DepthT>& a,
+                                                uint64_t b, uint64_t e, LaneT vis, LaneT all) {
+  const int lane = threadIdx.x & 31;
+  LaneT got = 0;
+  for (uint64_t e0 = b; e0 < e; e0 += 128) {
+    int32_t u[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const uint64_t idx = e0 + 32 * r + lane;
+      u[r] = idx < e ? __ldg(a.nbr + idx) : -1;
+    }
+    bool in[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) in[r] = u[r] >= 0 && in_frontier(a.fbits, u[r]);
+    LaneT x = 0;
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+      if (in[r]) x |= ld_lane(a.fr + u[r]);
+    got |= warp_or(x);
+    if (((got | vis) & all) == all) break;
+  }
+  return got;
+}
+
 template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
 __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
   MsCtl* c = a.ctl;
@@ -239,15 +267,24 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         const uint64_t b = (uint64_t)a.off[u] + (uint64_t)(ch - qc[lo]) * kMsTdChunk;
         const uint64_t ue = (uint64_t)a.off[u + 1];
         const uint64_t e = b + kMsTdChunk < ue ? b + kMsTdChunk : ue;
-        for (uint64_t e0 = b; e0 < e; e0 += 32) {
-          bool first = false;
-          int32_t v = 0;
-          if (e0 + lane < e) {
-            v = __ldg(a.nbr + e0 + lane);
-            const LaneT nb = f & ~ld_lane(a.visit + v);
-            if (nb) first = atomic_or_lane(a.acc + v, nb) == 0;
+        for (uint64_t e0 = b; e0 < e; e0 += 128) {
+          int32_t v[4];
+          LaneT vis[4];
+#pragma unroll
+          for (int r = 0; r < 4; r++) {
+            const uint64_t idx = e0 + 32 * r + lane;
+            v[r] = idx < e ? __ldg(a.nbr + idx) : -1;
           }
-          warp_append(touched, a.tq, first, v);
+#pragma unroll
+          for (int r = 0; r < 4; r++) vis[r] = v[r] >= 0 ? ld_lane(a.visit + v[r]) : all;
+          bool first[4];
+#pragma unroll
+          for (int r = 0; r < 4; r++) {
+            const LaneT nb = f & ~vis[r];
+            first[r] = v[r] >= 0 && nb && atomic_or_lane(a.acc + v[r], nb) == 0;
+          }
+#pragma unroll
+          for (int r = 0; r < 4; r++) warp_append(touched, a.tq, first[r], v[r]);
         }
       }
     } else {
@@ -286,16 +323,7 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
           mids &= mids - 1;
           const LaneT vt = shfl(vis, t);
           const uint64_t bt = shfl(b, t), et = shfl(e, t);
-          LaneT got = 0;
-          for (uint64_t e0 = bt; e0 < et; e0 += 32) {
-            LaneT x = 0;
-            if (e0 + lane < et) {
-              const int32_t u = __ldg(a.nbr + e0 + lane);
-              if (in_frontier(a.fbits, u)) x = ld_lane(a.fr + u);
-            }
-            got |= warp_or(x);
-            if (((got | vt) & all) == all) break;
-          }
+          const LaneT got = warp_gather_or(a, bt, et, vt, all);
           if (lane == t) nb = got & ~vt & all;
         }
         if (nb) {
@@ -318,16 +346,7 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         const uint64_t b = (uint64_t)a.off[v] + (uint64_t)(hc - a.hub_chunk[lo]) * kMsHubChunk;
         const uint64_t ve = (uint64_t)a.off[v + 1];
         const uint64_t e = b + kMsHubChunk < ve ? b + kMsHubChunk : ve;
-        LaneT got = 0;
-        for (uint64_t e0 = b; e0 < e; e0 += 32) {
-          LaneT x = 0;
-          if (e0 + lane < e) {
-            const int32_t u = __ldg(a.nbr + e0 + lane);
-            if (in_frontier(a.fbits, u)) x = ld_lane(a.fr + u);
-          }
-          got |= warp_or(x);
-          if (((got | vis) & all) == all) break;
-        }
+        const LaneT got = warp_gather_or(a, b, e, vis, all);
         const LaneT part = got & ~vis & all;
         bool first = false;
         if (lane == 0 && part) first = atomic_or_lane(a.acc + v, part) == 0;
