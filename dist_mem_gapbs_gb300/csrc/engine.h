@@ -24,6 +24,25 @@ void msbfs_release(MsState* ms);
 
 }  // namespace gbbfs
 
+struct gbbfs_graph;
+
+namespace gbbfs {
+
+// Asynchronous batch primitives of the multi-source search (msbfs.cu), used
+// by the query server.  Two depth buffers per handle; batches on one handle
+// run in stream order, batches on different handles overlap on the device.
+size_t ms_state_bytes(int64_t n, int64_t W, int depth_bytes);  // HBM a handle's state takes
+int ms_prepare(gbbfs_graph* g, int depth_bytes);   // allocate (or keep) the state
+int ms_lanes(const gbbfs_graph* g);
+int ms_launch(gbbfs_graph* g, int buf, const int32_t* sources, int k);
+bool ms_ready(gbbfs_graph* g, int buf);            // batch in `buf` has finished
+int ms_finish(gbbfs_graph* g, int buf);            // wait, then report its status
+void* ms_depth(gbbfs_graph* g, int buf);           // device rows of `buf`
+cudaEvent_t ms_done_event(gbbfs_graph* g, int buf);
+void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s);  // copies out of `buf` queued on s
+
+}  // namespace gbbfs
+
 #define GB_CUDA(call)                                                              \
   do {                                                                             \
     cudaError_t err_ = (call);                                                     \

@@ -92,6 +92,14 @@ void msbfs_release(MsState* ms) {
 // ---------------------------------------------------------------------------
 // Host side.
 
+// Lane words are allocated at 64 bits so both lane widths fit: visit, fr,
+// acc; queues q0/q1, chunk prefixes qc0/qc1 and tq; the frontier union; two
+// depth buffers of 64 rows; slack for the hub list and control blocks.
+size_t ms_state_bytes(int64_t n, int64_t W, int depth_bytes) {
+  return 3 * 8 * (size_t)n + 5 * 4 * (size_t)n + 4 * (size_t)W +
+         2 * (size_t)64 * n * depth_bytes + (16 << 20);
+}
+
 namespace {
 
 #define ms_error (::gbbfs::last_error())
@@ -137,9 +145,7 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
     g->ms = nullptr;
   }
   const int64_t n = g->n;
-  // Lane words are allocated at 64 bits so both lane widths fit.
-  const size_t need = 3 * 8 * (size_t)n + 3 * 4 * (size_t)n +
-                      2 * (size_t)64 * n * depth_bytes + (16 << 20);
+  const size_t need = ms_state_bytes(n, g->W, depth_bytes);
   size_t free_b = 0, total_b = 0;
   GB_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (need > free_b) {
@@ -390,6 +396,36 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
 }
 
 }  // namespace
+
+int ms_prepare(gbbfs_graph* g, int depth_bytes) {
+  GB_CUDA(cudaSetDevice(g->device));
+  return ensure_state(g, depth_bytes);
+}
+
+int ms_lanes(const gbbfs_graph* g) { return g->ms ? g->ms->cfg.lanes : MsConfig().lanes; }
+
+int ms_launch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
+  if (!g->ms || k < 1 || k > g->ms->cfg.lanes) return GBBFS_ERR_STATE;
+  return launch_batch(g, buf, sources, k);
+}
+
+bool ms_ready(gbbfs_graph* g, int buf) {
+  return cudaEventQuery(g->ms->computed[buf]) != cudaErrorNotReady;
+}
+
+int ms_finish(gbbfs_graph* g, int buf) {
+  int levels = 0;
+  return check_batch(g, buf, &levels);
+}
+
+void* ms_depth(gbbfs_graph* g, int buf) { return g->ms->depth[buf]; }
+
+cudaEvent_t ms_done_event(gbbfs_graph* g, int buf) { return g->ms->computed[buf]; }
+
+void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s) {
+  cudaEventRecord(g->ms->copied[buf], s);
+}
+
 }  // namespace gbbfs
 
 using namespace gbbfs;

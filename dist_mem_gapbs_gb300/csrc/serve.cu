@@ -1,0 +1,456 @@
+// Query server: (graph, source) BFS queries answered as they arrive.
+//
+// No counterpart in the reference.  A server holds a pool of resident graphs
+// (gbbfs_graph handles the caller created).  A host thread batches the
+// pending queries of each graph into the lanes of the multi-source search:
+// whenever one of a graph's two batch buffers is free, up to `lanes` queued
+// queries of that graph are launched together, so queries that arrive while
+// a batch is on the GPU join the next one.  Batches of different graphs run
+// on their graphs' own streams and overlap on the device.  The per-graph
+// search state (visit / frontier words, depth rows) is admitted against free
+// HBM and an optional byte budget; an idle graph gives its state back when
+// another graph needs the room.  mode 1 answers every query with its own
+// single-source search instead (the plain per-query baseline).
+//
+// Every result carries the query's timestamps on the server clock (submit,
+// launch, done) and a digest of its depth row: uint8 depths d[v] (255 =
+// unreached), checksum = sum over v of (d[v] + 1) * ((v + 1) * 0x9E3779B97F4A7C15)
+// mod 2^64, plus the number of reached vertices and the largest depth.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "engine.h"
+
+namespace gbbfs {
+
+struct RowStats {
+  unsigned long long sum;
+  unsigned long long reached;
+  unsigned int max_depth;
+  unsigned int pad;
+};
+
+// Digest of `rows` depth rows of n entries.  Depth type T: uint8 (255 =
+// unreached) or int32 (-1 = unreached, mapped to 255).  Optionally writes
+// the uint8 form to out8.
+template <typename T>
+__global__ void k_row_stats(const T* __restrict__ depth, int64_t n, int rows,
+                            RowStats* __restrict__ stats, uint8_t* __restrict__ out8) {
+  const int row = blockIdx.y;
+  if (row >= rows) return;
+  const T* d = depth + (int64_t)row * n;
+  unsigned long long sum = 0, reached = 0;
+  unsigned int mx = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    int x = (int)d[v];
+    unsigned int b = (x < 0 || x >= 255) ? 255u : (unsigned int)x;
+    if (out8) out8[(int64_t)row * n + v] = (uint8_t)b;
+    sum += (unsigned long long)(b + 1) * ((unsigned long long)(v + 1) * 0x9E3779B97F4A7C15ull);
+    if (b != 255u) {
+      reached++;
+      mx = b > mx ? b : mx;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    sum += __shfl_xor_sync(kFull, sum, o);
+    reached += __shfl_xor_sync(kFull, reached, o);
+    mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&stats[row].sum, sum);
+    atomicAdd(&stats[row].reached, reached);
+    atomicMax(&stats[row].max_depth, mx);
+  }
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Query {
+  uint64_t ticket;
+  int32_t graph;
+  int32_t source;
+  uint8_t* out;
+  double t_submit, t_start, t_done;
+  int batch;
+};
+
+struct Inflight {
+  bool busy = false;
+  std::vector<Query> q;
+  cudaEvent_t done = nullptr;
+};
+
+struct Slot {
+  gbbfs_graph* g = nullptr;
+  std::deque<Query> pending;
+  Inflight fl[2];
+  RowStats* d_stats = nullptr;   // 2 x 64
+  RowStats* h_stats = nullptr;   // pinned 2 x 64
+  uint8_t* d_plain = nullptr;    // plain mode: uint8 depth row
+  bool admitted = false;
+  double last_used = 0;
+};
+
+}  // namespace
+}  // namespace gbbfs
+
+using namespace gbbfs;
+
+struct gbbfs_server {
+  gbbfs_server_config cfg;
+  Clock::time_point t0;
+  std::vector<Slot> slots;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Query> inbox;
+  std::deque<gbbfs_result> done;
+  std::condition_variable done_cv;
+  uint64_t next_ticket = 1;
+  int64_t outstanding = 0;
+  bool stop = false;
+  bool started = false;
+  int device = 0;
+  int error = GBBFS_OK;
+  std::string error_msg;
+  std::thread worker;
+
+  double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+int64_t state_bytes_in_use(gbbfs_server* s) {
+  int64_t b = 0;
+  for (const Slot& sl : s->slots)
+    if (sl.admitted) b += (int64_t)ms_state_bytes(sl.g->n, sl.g->W, 1);
+  return b;
+}
+
+// Admission against free HBM and the configured budget; may evict idle slots.
+bool admit(gbbfs_server* s, size_t idx) {
+  Slot& sl = s->slots[idx];
+  if (sl.admitted) return true;
+  const int64_t need = (int64_t)ms_state_bytes(sl.g->n, sl.g->W, 1);
+  for (int pass = 0; pass < 2; pass++) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+    const bool hbm_ok = (int64_t)free_b > need + s->cfg.hbm_reserve_bytes;
+    const bool budget_ok = s->cfg.hbm_budget_bytes <= 0 ||
+                           state_bytes_in_use(s) + need <= s->cfg.hbm_budget_bytes;
+    if (hbm_ok && budget_ok) {
+      if (ms_prepare(sl.g, 1) != GBBFS_OK) return false;
+      sl.admitted = true;
+      return true;
+    }
+    if (pass == 1) break;
+    // Evict the least recently used idle slot that holds state.
+    int victim = -1;
+    for (size_t j = 0; j < s->slots.size(); j++) {
+      Slot& o = s->slots[j];
+      if (j == idx || !o.admitted || !o.pending.empty() || o.fl[0].busy || o.fl[1].busy) continue;
+      if (victim < 0 || o.last_used < s->slots[victim].last_used) victim = (int)j;
+    }
+    if (victim < 0) return false;
+    Slot& o = s->slots[victim];
+    cudaStreamSynchronize(o.g->stream);
+    msbfs_release(o.g->ms);
+    o.g->ms = nullptr;
+    o.admitted = false;
+  }
+  return false;
+}
+
+void complete(gbbfs_server* s, Slot& sl, Query& q, const RowStats& rs, int status) {
+  gbbfs_result r;
+  memset(&r, 0, sizeof r);
+  r.ticket = q.ticket;
+  r.graph_id = q.graph;
+  r.source = q.source;
+  r.status = status;
+  r.batch_size = q.batch;
+  r.submit_s = q.t_submit;
+  r.start_s = q.t_start;
+  r.done_s = q.t_done;
+  r.checksum = rs.sum;
+  r.reached = (int64_t)rs.reached;
+  r.max_depth = (int32_t)rs.max_depth;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->done.push_back(r);
+  s->outstanding--;
+  s->done_cv.notify_all();
+}
+
+// Harvest finished batches of a slot.
+void harvest(gbbfs_server* s, Slot& sl) {
+  for (int b = 0; b < 2; b++) {
+    Inflight& f = sl.fl[b];
+    if (!f.busy || cudaEventQuery(f.done) == cudaErrorNotReady) continue;
+    int st = ms_finish(sl.g, b);
+    const double t = s->now();
+    const size_t n = (size_t)sl.g->n;
+    for (size_t i = 0; i < f.q.size(); i++) {
+      Query& q = f.q[i];
+      q.t_done = t;
+      if (st == GBBFS_OK && q.out)
+        if (cudaMemcpy(q.out, static_cast<uint8_t*>(ms_depth(sl.g, b)) + i * n, n,
+                       cudaMemcpyDeviceToHost) != cudaSuccess)
+          st = GBBFS_ERR_CUDA;
+      complete(s, sl, q, sl.h_stats[64 * b + i], st);
+    }
+    f.q.clear();
+    f.busy = false;
+    sl.last_used = t;
+  }
+}
+
+// Launch the next batch of a slot into a free buffer.
+void launch(gbbfs_server* s, Slot& sl) {
+  for (int b = 0; b < 2 && !sl.pending.empty(); b++) {
+    Inflight& f = sl.fl[b];
+    if (f.busy) continue;
+    const int lanes = std::min<int>(ms_lanes(sl.g), std::max(1, s->cfg.max_batch));
+    const int k = (int)std::min<size_t>(sl.pending.size(), (size_t)lanes);
+    std::vector<int32_t> src(k);
+    const double t = s->now();
+    for (int i = 0; i < k; i++) {
+      f.q.push_back(sl.pending.front());
+      sl.pending.pop_front();
+      f.q.back().t_start = t;
+      f.q.back().batch = k;
+      src[i] = f.q.back().source;
+    }
+    int st = ms_launch(sl.g, b, src.data(), k);
+    if (st == GBBFS_OK) {
+      cudaStream_t str = sl.g->stream;
+      cudaMemsetAsync(sl.d_stats + 64 * b, 0, sizeof(RowStats) * k, str);
+      const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
+      k_row_stats<uint8_t><<<dim3(gx, k), 256, 0, str>>>(
+          static_cast<const uint8_t*>(ms_depth(sl.g, b)), sl.g->n, k, sl.d_stats + 64 * b,
+          nullptr);
+      cudaMemcpyAsync(sl.h_stats + 64 * b, sl.d_stats + 64 * b, sizeof(RowStats) * k,
+                      cudaMemcpyDeviceToHost, str);
+      ms_mark_copied(sl.g, b, str);
+      cudaEventRecord(f.done, str);
+      f.busy = true;
+    } else {
+      for (Query& q : f.q) {
+        q.t_done = s->now();
+        RowStats z = {0, 0, 0, 0};
+        complete(s, sl, q, z, st);
+      }
+      f.q.clear();
+    }
+  }
+}
+
+// Plain mode: one single-source search per query.
+void serve_plain(gbbfs_server* s, Slot& sl) {
+  if (sl.pending.empty()) return;
+  Query q = sl.pending.front();
+  sl.pending.pop_front();
+  q.t_start = s->now();
+  q.batch = 1;
+  int st = gbbfs_bfs_device(sl.g, q.source, 15, 18, 1, nullptr);
+  RowStats rs = {0, 0, 0, 0};
+  if (st == GBBFS_OK) {
+    const int32_t* dp = nullptr;
+    gbbfs_result_device_ptrs(sl.g, nullptr, &dp);
+    cudaStream_t str = sl.g->stream;
+    cudaMemsetAsync(sl.d_stats, 0, sizeof(RowStats), str);
+    const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
+    k_row_stats<int32_t><<<dim3(gx, 1), 256, 0, str>>>(dp, sl.g->n, 1, sl.d_stats,
+                                                       q.out ? sl.d_plain : nullptr);
+    cudaMemcpyAsync(sl.h_stats, sl.d_stats, sizeof(RowStats), cudaMemcpyDeviceToHost, str);
+    if (q.out) cudaMemcpyAsync(q.out, sl.d_plain, (size_t)sl.g->n, cudaMemcpyDeviceToHost, str);
+    if (cudaStreamSynchronize(str) != cudaSuccess) st = GBBFS_ERR_CUDA;
+    rs = sl.h_stats[0];
+  }
+  q.t_done = s->now();
+  sl.last_used = q.t_done;
+  complete(s, sl, q, rs, st);
+}
+
+void worker_loop(gbbfs_server* s) {
+  cudaSetDevice(s->device);
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      bool busy = false;
+      for (const Slot& sl : s->slots) busy = busy || sl.fl[0].busy || sl.fl[1].busy;
+      if (s->inbox.empty() && !busy) {
+        bool any_pending = false;
+        for (const Slot& sl : s->slots) any_pending = any_pending || !sl.pending.empty();
+        if (!any_pending) {
+          if (s->stop) return;
+          s->cv.wait_for(lk, std::chrono::microseconds(200));
+        }
+      }
+      while (!s->inbox.empty()) {
+        Query q = s->inbox.front();
+        s->inbox.pop_front();
+        s->slots[q.graph].pending.push_back(q);
+      }
+    }
+    bool any_busy = false;
+    for (size_t i = 0; i < s->slots.size(); i++) {
+      Slot& sl = s->slots[i];
+      if (s->cfg.mode == 1) {
+        serve_plain(s, sl);
+        continue;
+      }
+      harvest(s, sl);
+      if (!sl.pending.empty()) {
+        if (admit(s, i)) {
+          launch(s, sl);
+        } else {
+          bool others = false;
+          for (const Slot& o : s->slots) others = others || o.fl[0].busy || o.fl[1].busy;
+          if (!others) {
+            // Nothing in flight will free memory: the queries cannot be served.
+            last_error() = "query state does not fit in free HBM / the server budget";
+            while (!sl.pending.empty()) {
+              Query q = sl.pending.front();
+              sl.pending.pop_front();
+              q.t_start = q.t_done = s->now();
+              RowStats z = {0, 0, 0, 0};
+              complete(s, sl, q, z, GBBFS_ERR_NOMEM);
+            }
+          }
+        }
+      }
+      any_busy = any_busy || sl.fl[0].busy || sl.fl[1].busy;
+    }
+    if (any_busy) std::this_thread::sleep_for(std::chrono::microseconds(5));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out) {
+  if (!out) return GBBFS_ERR_ARG;
+  *out = nullptr;
+  gbbfs_server* s = new (std::nothrow) gbbfs_server();
+  if (!s) return GBBFS_ERR_NOMEM;
+  memset(&s->cfg, 0, sizeof s->cfg);
+  s->cfg.max_batch = 64;
+  if (cfg) s->cfg = *cfg;
+  if (s->cfg.max_batch <= 0) s->cfg.max_batch = 64;
+  if (s->cfg.mode != 0 && s->cfg.mode != 1) {
+    delete s;
+    last_error() = "server mode must be 0 (batched) or 1 (plain)";
+    return GBBFS_ERR_ARG;
+  }
+  s->t0 = Clock::now();
+  cudaGetDevice(&s->device);
+  *out = s;
+  return GBBFS_OK;
+}
+
+int gbbfs_server_add_graph(gbbfs_server* s, gbbfs_graph* g, int32_t* graph_id) {
+  if (!s || !g || !graph_id) return GBBFS_ERR_ARG;
+  if (s->started) {
+    last_error() = "graphs must be added before the first query";
+    return GBBFS_ERR_STATE;
+  }
+  Slot sl;
+  sl.g = g;
+  GB_CUDA(cudaMalloc(&sl.d_stats, sizeof(RowStats) * 128));
+  GB_CUDA(cudaHostAlloc(&sl.h_stats, sizeof(RowStats) * 128, cudaHostAllocDefault));
+  GB_CUDA(cudaMalloc(&sl.d_plain, std::max<size_t>((size_t)g->n, 256)));
+  for (int b = 0; b < 2; b++)
+    GB_CUDA(cudaEventCreateWithFlags(&sl.fl[b].done, cudaEventDisableTiming));
+  s->slots.push_back(std::move(sl));
+  *graph_id = (int32_t)s->slots.size() - 1;
+  return GBBFS_OK;
+}
+
+int gbbfs_server_submit(gbbfs_server* s, int32_t graph_id, int32_t source, uint8_t* depth_out,
+                        uint64_t* ticket) {
+  if (!s || graph_id < 0 || graph_id >= (int32_t)s->slots.size()) return GBBFS_ERR_ARG;
+  if (source < 0 || source >= s->slots[graph_id].g->n) {
+    last_error() = "source out of range";
+    return GBBFS_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop) return GBBFS_ERR_STATE;
+  if (!s->started) {
+    s->started = true;
+    s->worker = std::thread(worker_loop, s);
+  }
+  Query q;
+  q.ticket = s->next_ticket++;
+  q.graph = graph_id;
+  q.source = source;
+  q.out = depth_out;
+  q.t_submit = s->now();
+  q.t_start = q.t_done = 0;
+  q.batch = 0;
+  s->inbox.push_back(q);
+  s->outstanding++;
+  if (ticket) *ticket = q.ticket;
+  s->cv.notify_one();
+  return GBBFS_OK;
+}
+
+int gbbfs_server_poll(gbbfs_server* s, gbbfs_result* out, int32_t max, int32_t* count,
+                      int32_t wait_us) {
+  if (!s || !count || (max > 0 && !out)) return GBBFS_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (s->done.empty() && wait_us > 0)
+    s->done_cv.wait_for(lk, std::chrono::microseconds(wait_us), [&] { return !s->done.empty(); });
+  int32_t c = 0;
+  while (c < max && !s->done.empty()) {
+    out[c++] = s->done.front();
+    s->done.pop_front();
+  }
+  *count = c;
+  return GBBFS_OK;
+}
+
+int gbbfs_server_drain(gbbfs_server* s, int32_t timeout_ms) {
+  if (!s) return GBBFS_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  const bool ok = s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms),
+                                      [&] { return s->outstanding == 0; });
+  return ok ? GBBFS_OK : GBBFS_ERR_TIMEOUT;
+}
+
+double gbbfs_server_clock(const gbbfs_server* s) { return s ? s->now() : 0.0; }
+
+int gbbfs_server_close(gbbfs_server* s) {
+  if (!s) return GBBFS_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv.notify_all();
+  }
+  if (s->worker.joinable()) s->worker.join();
+  for (Slot& sl : s->slots) {
+    if (sl.g && sl.g->stream) cudaStreamSynchronize(sl.g->stream);
+    cudaFree(sl.d_stats);
+    cudaFreeHost(sl.h_stats);
+    cudaFree(sl.d_plain);
+    for (int b = 0; b < 2; b++)
+      if (sl.fl[b].done) cudaEventDestroy(sl.fl[b].done);
+  }
+  delete s;
+  return GBBFS_OK;
+}
+
+}  // extern "C"

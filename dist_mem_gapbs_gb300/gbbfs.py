@@ -33,7 +33,9 @@ EXPORTS = (
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
     "gbbfs_append_bfs_output", "gbbfs_msbfs", "gbbfs_msbfs_device", "gbbfs_msbfs_set_config",
-    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune",
+    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_server_open",
+    "gbbfs_server_add_graph", "gbbfs_server_submit", "gbbfs_server_poll", "gbbfs_server_drain",
+    "gbbfs_server_clock", "gbbfs_server_close",
 )
 
 
@@ -113,6 +115,13 @@ def lib():
             "gbbfs_msbfs_set_config": (I, [P, P]),
             "gbbfs_msbfs_get_config": (I, [P, P]),
             "gbbfs_msbfs_autotune": (I, [P, P, i64, I, P]),
+            "gbbfs_server_open": (I, [P, PP]),
+            "gbbfs_server_add_graph": (I, [P, P, P]),
+            "gbbfs_server_submit": (I, [P, i32, i32, P, P]),
+            "gbbfs_server_poll": (I, [P, P, i32, P, i32]),
+            "gbbfs_server_drain": (I, [P, i32]),
+            "gbbfs_server_clock": (ctypes.c_double, [P]),
+            "gbbfs_server_close": (I, [P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -376,3 +385,90 @@ def msbfs_autotune(g, sample, depth_bytes=1):
     _check(lib().gbbfs_msbfs_autotune(g.handle, _p(src), len(src), int(depth_bytes),
                                       ctypes.byref(c)), "msbfs_autotune")
     return c.as_dict()
+
+
+# ---------------------------------------------------------------------------
+# Query server.
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("hbm_budget_bytes", ctypes.c_int64), ("hbm_reserve_bytes", ctypes.c_int64)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_uint64), ("graph_id", ctypes.c_int32),
+                ("source", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("batch_size", ctypes.c_int32), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("checksum", ctypes.c_uint64), ("reached", ctypes.c_int64),
+                ("max_depth", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+def depth_checksum(depth_u8):
+    """Host restatement of the server's digest of a uint8 depth row."""
+    d = np.asarray(depth_u8, dtype=np.uint64)
+    v = np.arange(1, len(d) + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        mix = v * np.uint64(0x9E3779B97F4A7C15)
+        return int(np.sum((d + np.uint64(1)) * mix, dtype=np.uint64))
+
+
+class Server:
+    """(graph, source) queries answered as they arrive (see include/gbbfs.h)."""
+
+    PLAIN = 1
+    BATCHED = 0
+
+    def __init__(self, mode=0, max_batch=64, hbm_budget_bytes=0, hbm_reserve_bytes=0):
+        cfg = ServerConfig(mode, max_batch, hbm_budget_bytes, hbm_reserve_bytes)
+        h = ctypes.c_void_p()
+        _check(lib().gbbfs_server_open(ctypes.byref(cfg), ctypes.byref(h)), "server_open")
+        self._h = h
+        self._graphs = []
+        self._keep = {}
+
+    def add_graph(self, g):
+        gid = ctypes.c_int32()
+        _check(lib().gbbfs_server_add_graph(self._h, g.handle, ctypes.byref(gid)), "add_graph")
+        self._graphs.append(g)
+        return gid.value
+
+    def submit(self, graph_id, source, out=None):
+        t = ctypes.c_uint64()
+        _check(lib().gbbfs_server_submit(self._h, int(graph_id), int(source), _p(out),
+                                         ctypes.byref(t)), "server_submit")
+        if out is not None:
+            self._keep[t.value] = out
+        return t.value
+
+    def poll(self, max_results=1024, wait_us=0):
+        buf = (Result * max_results)()
+        cnt = ctypes.c_int32()
+        _check(lib().gbbfs_server_poll(self._h, buf, max_results, ctypes.byref(cnt),
+                                       int(wait_us)), "server_poll")
+        out = []
+        for i in range(cnt.value):
+            r = buf[i]
+            self._keep.pop(r.ticket, None)
+            out.append(dict(ticket=r.ticket, graph_id=r.graph_id, source=r.source,
+                            status=r.status, batch_size=r.batch_size, submit_s=r.submit_s,
+                            start_s=r.start_s, done_s=r.done_s, checksum=r.checksum,
+                            reached=r.reached, max_depth=r.max_depth))
+        return out
+
+    def drain(self, timeout_ms=600000):
+        _check(lib().gbbfs_server_drain(self._h, int(timeout_ms)), "server_drain")
+
+    def clock(self):
+        return lib().gbbfs_server_clock(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            lib().gbbfs_server_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

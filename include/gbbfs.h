@@ -156,6 +156,56 @@ int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg);
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,
                          gbbfs_ms_config* best);
 
+/* ---- Query server (no reference counterpart) ----
+ * (graph, source) queries answered as they arrive.  A host thread batches
+ * the pending queries of each resident graph into the lanes of the
+ * multi-source search: whenever one of a graph's two batch buffers is free,
+ * up to max_batch queued queries of that graph launch together, so queries
+ * that arrive while a batch runs join the next one, and batches of different
+ * graphs overlap on the device.  Per-graph search state is admitted against
+ * free HBM (and the optional budget); an idle graph's state is released when
+ * another graph needs the room.  Results carry timestamps for latency and a
+ * digest of the depth row; the row itself is copied out when the query gives
+ * a host buffer.  The server drives the graph handles it is given until it
+ * is closed: do not call other functions on them meanwhile. */
+typedef struct gbbfs_server gbbfs_server;
+
+typedef struct gbbfs_server_config {
+  int32_t mode;              /* 0: batched multi-source; 1: one plain search per query */
+  int32_t max_batch;         /* queries per batch, <= lanes (default 64)         */
+  int64_t hbm_budget_bytes;  /* cap on per-graph search state, 0 = none          */
+  int64_t hbm_reserve_bytes; /* free HBM to leave untouched                      */
+} gbbfs_server_config;
+
+typedef struct gbbfs_result {
+  uint64_t ticket;
+  int32_t graph_id;
+  int32_t source;
+  int32_t status;      /* GBBFS_OK or the error that ended the query             */
+  int32_t batch_size;  /* queries in the batch that answered it                  */
+  double submit_s, start_s, done_s;  /* server clock (gbbfs_server_clock)       */
+  /* digest of the uint8 depth row d (255 = unreached):
+   * sum over v of (d[v] + 1) * ((v + 1) * 0x9E3779B97F4A7C15), mod 2^64 */
+  uint64_t checksum;
+  int64_t reached;     /* vertices with a depth                                  */
+  int32_t max_depth;
+  int32_t pad;
+} gbbfs_result;
+
+int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out);
+int gbbfs_server_add_graph(gbbfs_server* s, gbbfs_graph* g, int32_t* graph_id);
+/* depth_out: host buffer of n bytes for the uint8 depth row, or NULL. */
+int gbbfs_server_submit(gbbfs_server* s, int32_t graph_id, int32_t source, uint8_t* depth_out,
+                        uint64_t* ticket);
+/* Up to max finished results; waits up to wait_us for the first one. */
+int gbbfs_server_poll(gbbfs_server* s, gbbfs_result* out, int32_t max, int32_t* count,
+                      int32_t wait_us);
+/* Wait until every submitted query has a result (GBBFS_ERR_TIMEOUT otherwise). */
+int gbbfs_server_drain(gbbfs_server* s, int32_t timeout_ms);
+/* Seconds since the server was opened (the clock of the result timestamps). */
+double gbbfs_server_clock(const gbbfs_server* s);
+int gbbfs_server_close(gbbfs_server* s);
+
 /* Human-readable name of a status code. */
 const char* gbbfs_strerror(int status);
 

@@ -1,0 +1,122 @@
+"""Query server: every result must be the same alone and in a mix of
+concurrent queries on several resident graphs, and equal to the single-source
+search (pinned to the reference by test_bfs_gpu)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def u8(depth32):
+    d = depth32.astype(np.int64)
+    d[d < 0] = 255
+    return d.astype(np.uint8)
+
+
+@pytest.fixture(scope="module")
+def pool(native):
+    specs = [(12, 16, False), (12, 16, True), (14, 8, False)]
+    graphs = []
+    for sc, k, uni in specs:
+        off, nbr = native.make_graph(sc, k, uni)
+        graphs.append((off, native.Graph(off, nbr)))
+    yield graphs
+    for _, g in graphs:
+        g.close()
+
+
+def expected(native, pool):
+    exp = {}
+    for gid, (off, g) in enumerate(pool):
+        for s in native.pick_sources(off, 40):
+            d = u8(native.DOBFS(g, int(s), depth=True)[1])
+            exp[(gid, int(s))] = d
+    return exp
+
+
+def run_queries(native, server, queries, n_of, with_rows):
+    rows = {}
+    for i, (gid, s) in enumerate(queries):
+        out = np.empty(n_of[gid], np.uint8) if with_rows else None
+        t = server.submit(gid, s, out)
+        rows[t] = (gid, s, out)
+    server.drain()
+    res = []
+    while True:
+        got = server.poll(4096)
+        if not got:
+            break
+        res += got
+    assert len(res) == len(queries)
+    return res, rows
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_alone_and_mixed(native, pool, mode):
+    exp = expected(native, pool)
+    n_of = [g.n for _, g in pool]
+    keys = list(exp)
+    with native.Server(mode=mode) as srv:
+        ids = [srv.add_graph(g) for _, g in pool]
+        assert ids == [0, 1, 2]
+        # alone: one query at a time
+        alone = {}
+        for key in keys[::7]:
+            res, rows = run_queries(native, srv, [key], n_of, True)
+            r = res[0]
+            assert r["status"] == 0 and r["batch_size"] == 1
+            alone[key] = (r["checksum"], rows[r["ticket"]][2].copy())
+        # mixed: every query of every graph, shuffled, repeats included
+        rng = np.random.default_rng(9)
+        mix = [keys[i] for i in rng.permutation(len(keys))] + keys[:25]
+        res, rows = run_queries(native, srv, mix, n_of, True)
+        batched = 0
+        for r in res:
+            key = (r["graph_id"], r["source"])
+            row = rows[r["ticket"]][2]
+            assert r["status"] == 0
+            assert np.array_equal(row, exp[key])
+            assert r["checksum"] == native.depth_checksum(exp[key])
+            assert r["reached"] == int((exp[key] != 255).sum())
+            assert r["max_depth"] == int(exp[key][exp[key] != 255].max())
+            assert r["submit_s"] <= r["start_s"] <= r["done_s"]
+            if key in alone:
+                assert alone[key][0] == r["checksum"]
+                assert np.array_equal(alone[key][1], row)
+            batched = max(batched, r["batch_size"])
+        if mode == 0:
+            assert batched > 1      # queries really shared batches
+        else:
+            assert batched == 1
+
+
+def test_admission_budget(native, pool):
+    """A budget that holds one graph's search state at a time: graphs take
+    turns, every answer still exact."""
+    exp = expected(native, pool)
+    n_of = [g.n for _, g in pool]
+    biggest = max(g.n for _, g in pool)
+    W = (biggest + 31) // 32
+    budget = 3 * 8 * biggest + 5 * 4 * biggest + 4 * W + 2 * 64 * biggest + (16 << 20)
+    with native.Server(mode=0, hbm_budget_bytes=budget) as srv:
+        for _, g in pool:
+            srv.add_graph(g)
+        keys = list(exp)
+        res, _ = run_queries(native, srv, keys + keys[::-1], n_of, False)
+        for r in res:
+            assert r["status"] == 0
+            assert r["checksum"] == native.depth_checksum(exp[(r["graph_id"], r["source"])])
+
+
+def test_server_rejects(native, pool):
+    with native.Server() as srv:
+        gid = srv.add_graph(pool[0][1])
+        with pytest.raises(native.GbbfsError):
+            srv.submit(gid, pool[0][1].n + 3)
+        with pytest.raises(native.GbbfsError):
+            srv.submit(gid + 5, 0)
+        srv.submit(gid, int(native.pick_sources(pool[0][0], 1)[0]))
+        with pytest.raises(native.GbbfsError) as e:
+            srv.add_graph(pool[1][1])
+        assert e.value.status == native.ERR_STATE
+        srv.drain()
