@@ -35,7 +35,7 @@ EXPORTS = (
     "gbbfs_append_bfs_output", "gbbfs_msbfs", "gbbfs_msbfs_device", "gbbfs_msbfs_set_config",
     "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_server_open",
     "gbbfs_server_add_graph", "gbbfs_server_submit", "gbbfs_server_poll", "gbbfs_server_drain",
-    "gbbfs_server_clock", "gbbfs_server_close",
+    "gbbfs_server_clock", "gbbfs_server_close", "gbbfs_bfs_noalloc",
 )
 
 
@@ -122,6 +122,7 @@ def lib():
             "gbbfs_server_drain": (I, [P, i32]),
             "gbbfs_server_clock": (ctypes.c_double, [P]),
             "gbbfs_server_close": (I, [P]),
+            "gbbfs_bfs_noalloc": (I, [P, P, i64, i64, i32, I, I, P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
