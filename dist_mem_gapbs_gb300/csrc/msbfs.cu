@@ -330,7 +330,14 @@ int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
   return GBBFS_OK;
 }
 
-int check_batch(gbbfs_graph* g, int buf, int* levels) {
+// Levels and per-direction device time of finished batches.
+struct MsTally {
+  int levels = 0;
+  int td_levels = 0, bu_levels = 0;
+  double td_ms = 0, bu_ms = 0;
+};
+
+int check_batch(gbbfs_graph* g, int buf, MsTally* t) {
   MsState* ms = g->ms;
   GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
   const MsCtl& c = ms->h_ctl[buf];
@@ -340,7 +347,19 @@ int check_batch(gbbfs_graph* g, int buf, int* levels) {
                    : "a depth exceeds the uint8 output range (use 4-byte depths)";
     return c.error;
   }
-  if (levels) *levels = std::max(*levels, c.levels);
+  if (t) {
+    t->levels = std::max(t->levels, c.levels);
+    for (int l = 1; l <= c.levels && l < kMsTimedLevels; l++) {
+      const double ms_l = (double)(c.level_end[l] - c.level_end[l - 1]) * 1e-6;
+      if (c.level_bu[l]) {
+        t->bu_ms += ms_l;
+        t->bu_levels++;
+      } else {
+        t->td_ms += ms_l;
+        t->td_levels++;
+      }
+    }
+  }
   return GBBFS_OK;
 }
 
@@ -360,7 +379,7 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
     return GBBFS_ERR_ARG;
   }
   const size_t per_src = (size_t)g->n * depth_bytes;
-  int levels = 0;
+  MsTally tally;
   GB_CUDA(cudaEventRecord(ms->ev0, g->stream));
   for (int64_t b = 0; b < nb; b++) {
     const int buf = (int)(b & 1);
@@ -374,12 +393,12 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
                               ms->copy_stream));
       GB_CUDA(cudaEventRecord(ms->copied[buf], ms->copy_stream));
     }
-    if (b >= 1) GB_TRY(check_batch(g, buf ^ 1, &levels));
+    if (b >= 1) GB_TRY(check_batch(g, buf ^ 1, &tally));
     ms->last_buf = buf;
     ms->last_k = kb;
   }
   GB_CUDA(cudaEventRecord(ms->ev1, g->stream));
-  GB_TRY(check_batch(g, ms->last_buf, &levels));
+  GB_TRY(check_batch(g, ms->last_buf, &tally));
   GB_CUDA(cudaStreamSynchronize(ms->copy_stream));
   GB_CUDA(cudaStreamSynchronize(g->stream));
   if (st) {
@@ -387,10 +406,14 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
     GB_CUDA(cudaEventElapsedTime(&ms_elapsed, ms->ev0, ms->ev1));
     st->device_ms = ms_elapsed;
     st->batches = (int32_t)nb;
-    st->levels = levels;
+    st->levels = tally.levels;
     st->lanes = lanes;
     st->batch = ms->cfg.batch;
     st->alpha = ms->cfg.alpha;
+    st->td_levels = tally.td_levels;
+    st->bu_levels = tally.bu_levels;
+    st->td_ms = tally.td_ms;
+    st->bu_ms = tally.bu_ms;
   }
   return GBBFS_OK;
 }
@@ -414,8 +437,7 @@ bool ms_ready(gbbfs_graph* g, int buf) {
 }
 
 int ms_finish(gbbfs_graph* g, int buf) {
-  int levels = 0;
-  return check_batch(g, buf, &levels);
+  return check_batch(g, buf, nullptr);
 }
 
 void* ms_depth(gbbfs_graph* g, int buf) { return g->ms->depth[buf]; }

@@ -17,11 +17,13 @@
 //   expand   top-down (frontier summed degree <= m / alpha): work items of
 //            kMsTdChunk edges of one frontier vertex, a warp per item,
 //            atomicOr of fr[u] & ~visit[v] into acc[v];
-//            bottom-up: a warp per 32 consecutive vertices — thread per vertex
-//            up to kMsLight neighbours, the whole warp per vertex up to
-//            kMsHubDeg, early exit once every lane of v is found — plus the
-//            adjacency of hubs cut into kMsHubChunk-edge items merged into
-//            acc by atomicOr;
+//            bottom-up: a warp per 32 consecutive vertices — the concatenated
+//            adjacency of the tile's unfinished vertices of degree up to
+//            kMsSmall streamed 32 edges per lane-step into per-vertex words in
+//            shared memory, the whole warp per vertex up to kMsHubDeg with
+//            early exit once every lane of v is found — plus the adjacency
+//            of hubs cut into kMsHubChunk-edge items merged into acc by
+//            atomicOr;
 //   clear    the old frontier (fr, fbits);
 //   install  the new frontier from acc, queued with its work-chunk prefix.
 // Grid barriers between the phases spin on a generation word with a time
@@ -32,7 +34,8 @@
 
 namespace gbbfs {
 
-constexpr int kMsLight = 32;
+constexpr int kMsTimedLevels = 64;   // levels whose end time and direction are kept
+constexpr int kMsSmall = 256;
 constexpr int kMsHubDeg = 2048;
 constexpr int kMsHubChunk = 2048;
 constexpr int kMsTdChunk = 1024;
@@ -46,6 +49,8 @@ struct MsCtl {
   int error;
   int levels;
   unsigned long long t_begin, t_end;
+  unsigned long long level_end[kMsTimedLevels];   // %globaltimer at the end of each level
+  int level_bu[kMsTimedLevels];                    // 1 when the level ran bottom-up
 };
 
 template <typename OffT, typename LaneT, typename DepthT>
@@ -202,6 +207,7 @@ __device__ __forceinline__ LaneT warp_gather_or(const MsArgs<OffT, LaneT, DepthT
 
 template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
 __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
+  __shared__ LaneT tile_acc[kWarpsPerCta][32];
   MsCtl* c = a.ctl;
   const unsigned nblocks = gridDim.x;
   const int lane = threadIdx.x & 31;
@@ -235,6 +241,7 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
     }
   }
   if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+  if (tid == 0) c->level_end[0] = globaltimer();
 
   int cur = 0;
   for (int level = 1;; level++) {
@@ -301,23 +308,52 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         const bool need = ((vis & all) != all) && e > b;
         const uint64_t deg = e - b;
         LaneT nb = 0;
-        if (need && deg <= kMsLight) {
-          LaneT got = 0;
-          for (uint64_t pos = b; pos < e; pos += kBatchN) {
-            int32_t u[kBatchN];
+        // Small vertices: the warp streams their concatenated adjacency,
+        // kBatchN/2 x 32 edges per round, loads issued together; bits are
+        // ORed into per-vertex words in shared memory.
+        const bool small = need && deg <= (uint64_t)kMsSmall;
+        const unsigned sd = small ? (unsigned)deg : 0u;
+        const unsigned sincl = warp_inclusive_sum(sd, lane);
+        const unsigned sstart = sincl - sd;
+        const unsigned stotal = __shfl_sync(kFull, sincl, 31);
+        LaneT* tacc = tile_acc[threadIdx.x >> 5];
+        tacc[lane] = 0;
+        __syncwarp();
+        constexpr int kR = kBatchN / 2 > 0 ? kBatchN / 2 : 1;
+        for (unsigned t0 = 0; t0 < stotal; t0 += 32 * kR) {
+          int seg[kR];
+          int32_t u[kR];
 #pragma unroll
-            for (int t = 0; t < kBatchN; t++) u[t] = pos + t < e ? __ldg(a.nbr + pos + t) : -1;
-            bool in[kBatchN];
+          for (int r = 0; r < kR; r++) {
+            const unsigned t = t0 + 32 * r + lane;
+            const unsigned tc = t < stotal ? t : stotal - 1;
+            // last vertex of the tile whose stream starts at or before tc
+            // (every lane takes part in the shuffles)
+            int lo = 0;
 #pragma unroll
-            for (int t = 0; t < kBatchN; t++) in[t] = u[t] >= 0 && in_frontier(a.fbits, u[t]);
-#pragma unroll
-            for (int t = 0; t < kBatchN; t++)
-              if (in[t]) got |= ld_lane(a.fr + u[t]);
-            if (((got | vis) & all) == all) break;
+            for (int step = 16; step; step >>= 1) {
+              const unsigned st = __shfl_sync(kFull, sstart, lo + step);
+              if (st <= tc) lo += step;
+            }
+            const uint64_t bs = shfl(b, lo);
+            const unsigned ss = __shfl_sync(kFull, sstart, lo);
+            seg[r] = t < stotal ? lo : -1;
+            u[r] = t < stotal ? __ldg(a.nbr + bs + (t - ss)) : -1;
           }
-          nb = got & ~vis & all;
+          bool in[kR];
+#pragma unroll
+          for (int r = 0; r < kR; r++) in[r] = u[r] >= 0 && in_frontier(a.fbits, u[r]);
+#pragma unroll
+          for (int r = 0; r < kR; r++) {
+            if (in[r]) {
+              const LaneT x = ld_lane(a.fr + u[r]);
+              if (x) atomic_or_lane(tacc + seg[r], x);
+            }
+          }
         }
-        unsigned mids = __ballot_sync(kFull, need && deg > kMsLight && deg <= kMsHubDeg);
+        __syncwarp();
+        if (small) nb = tacc[lane] & ~vis & all;
+        unsigned mids = __ballot_sync(kFull, need && deg > kMsSmall && deg <= kMsHubDeg);
         while (mids) {
           const int t = __ffs(mids) - 1;
           mids &= mids - 1;
@@ -419,7 +455,13 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
     }
     if (!grid_barrier(c, nblocks, a.limit_ns)) return;
     cur ^= 1;
-    if (tid == 0) c->levels = level;
+    if (tid == 0) {
+      c->levels = level;
+      if (level < kMsTimedLevels) {
+        c->level_end[level] = globaltimer();
+        c->level_bu[level] = bottom_up ? 1 : 0;
+      }
+    }
   }
   if (tid == 0) c->t_end = globaltimer();
 }

@@ -76,7 +76,9 @@ class MsConfig(ctypes.Structure):
 class MsStats(ctypes.Structure):
     _fields_ = [("device_ms", ctypes.c_double), ("batches", ctypes.c_int32),
                 ("levels", ctypes.c_int32), ("lanes", ctypes.c_int32),
-                ("batch", ctypes.c_int32), ("alpha", ctypes.c_int32)]
+                ("batch", ctypes.c_int32), ("alpha", ctypes.c_int32),
+                ("td_levels", ctypes.c_int32), ("bu_levels", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("td_ms", ctypes.c_double), ("bu_ms", ctypes.c_double)]
 
 
 _lib = None

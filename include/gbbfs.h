@@ -150,6 +150,9 @@ typedef struct gbbfs_ms_stats {
   int32_t batches;
   int32_t levels;    /* deepest level of any batch                       */
   int32_t lanes, batch, alpha;  /* configuration used                     */
+  int32_t td_levels, bu_levels; /* levels run top-down / bottom-up (all batches) */
+  int32_t pad;
+  double td_ms, bu_ms;          /* device time spent in them            */
 } gbbfs_ms_stats;
 
 /* BFS depths from k sources.  depth_out (host) receives k rows of n entries,
