@@ -335,6 +335,7 @@ struct MsTally {
   int levels = 0;
   int td_levels = 0, bu_levels = 0;
   double td_ms = 0, bu_ms = 0;
+  double phase[kMsPhases] = {};
 };
 
 int check_batch(gbbfs_graph* g, int buf, MsTally* t) {
@@ -348,6 +349,7 @@ int check_batch(gbbfs_graph* g, int buf, MsTally* t) {
     return c.error;
   }
   if (t) {
+    for (int p = 0; p < kMsPhases; p++) t->phase[p] += (double)c.phase_cycles[p];
     t->levels = std::max(t->levels, c.levels);
     for (int l = 1; l <= c.levels && l < kMsTimedLevels; l++) {
       const double ms_l = (double)(c.level_end[l] - c.level_end[l - 1]) * 1e-6;
@@ -414,6 +416,10 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
     st->bu_levels = tally.bu_levels;
     st->td_ms = tally.td_ms;
     st->bu_ms = tally.bu_ms;
+    double total = 0;
+    for (int p = 0; p < kMsPhases; p++) total += tally.phase[p];
+    for (int p = 0; p < kMsPhases && p < 8; p++)
+      st->phase_share[p] = total > 0 ? tally.phase[p] / total : 0.0;
   }
   return GBBFS_OK;
 }

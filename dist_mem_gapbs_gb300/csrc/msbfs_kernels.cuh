@@ -35,6 +35,11 @@
 namespace gbbfs {
 
 constexpr int kMsTimedLevels = 64;   // levels whose end time and direction are kept
+// Phases whose warp time the kernel accounts (SM cycles summed over warps).
+enum MsPhase {
+  kPhTopDown = 0, kPhSmall, kPhMid, kPhWrite, kPhHub, kPhClear, kPhInstall, kPhBarrier,
+  kMsPhases
+};
 constexpr int kMsSmall = 256;
 constexpr int kMsHubDeg = 2048;
 constexpr int kMsHubChunk = 2048;
@@ -51,6 +56,7 @@ struct MsCtl {
   unsigned long long t_begin, t_end;
   unsigned long long level_end[kMsTimedLevels];   // %globaltimer at the end of each level
   int level_bu[kMsTimedLevels];                    // 1 when the level ran bottom-up
+  unsigned long long phase_cycles[kMsPhases];      // SM cycles per phase, summed over warps
 };
 
 template <typename OffT, typename LaneT, typename DepthT>
@@ -221,6 +227,23 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
   const int max_level = sizeof(DepthT) == 1 ? 254 : 0x7ffffffe;
   const int64_t hub_chunks = a.nhubs ? (int64_t)a.hub_chunk[a.nhubs] : 0;
   if (tid == 0) c->t_begin = globaltimer();
+  // Warp time per phase (for the stats): lane 0 of each warp adds its SM
+  // cycles since the previous mark.
+  __shared__ unsigned long long ph_acc[kMsPhases];
+  if (threadIdx.x < kMsPhases) ph_acc[threadIdx.x] = 0;
+  __syncthreads();
+  long long ph_t = clock64();
+  auto mark = [&](int phase) {
+    const long long now = clock64();
+    if (lane == 0) atomicAdd(&ph_acc[phase], (unsigned long long)(now - ph_t));
+    ph_t = now;
+  };
+  // Grid barrier; the time spent waiting in it is its own phase.
+  auto barrier = [&]() {
+    const bool ok = grid_barrier(c, nblocks, a.limit_ns);
+    mark(kPhBarrier);
+    return ok;
+  };
 
   // Sources: lane i starts at sources[i] with depth 0.  A vertex that is the
   // source of several lanes is queued once.
@@ -294,6 +317,7 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
           for (int r = 0; r < 4; r++) warp_append(touched, a.tq, first[r], v[r]);
         }
       }
+      mark(kPhTopDown);
     } else {
       // Bottom-up over tiles of 32 consecutive vertices.
       for (int64_t v0 = warp << 5; v0 < a.n; v0 += nwarps << 5) {
@@ -353,6 +377,7 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         }
         __syncwarp();
         if (small) nb = tacc[lane] & ~vis & all;
+        mark(kPhSmall);
         unsigned mids = __ballot_sync(kFull, need && deg > kMsSmall && deg <= kMsHubDeg);
         while (mids) {
           const int t = __ffs(mids) - 1;
@@ -362,12 +387,14 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
           const LaneT got = warp_gather_or(a, bt, et, vt, all);
           if (lane == t) nb = got & ~vt & all;
         }
+        mark(kPhMid);
         if (nb) {
           a.visit[v] = vis | nb;
           a.acc[v] = nb;
         }
         write_depths(a.depth, a.n, v, nb, level);
         warp_append(touched, a.tq, nb != 0, (int32_t)v);
+        mark(kPhWrite);
       }
       // Hubs: their adjacency cut into work items, merged by atomicOr.
       for (int64_t hc = warp; hc < hub_chunks; hc += nwarps) {
@@ -388,8 +415,9 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         if (lane == 0 && part) first = atomic_or_lane(a.acc + v, part) == 0;
         warp_append(touched, a.tq, first, v);
       }
+      mark(kPhHub);
     }
-    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+    if (!barrier()) return;
 
     // Clear the old frontier; reset the counters the next level fills.
     for (int64_t i = tid; i < F; i += nthreads) {
@@ -402,7 +430,8 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
       c->q_edges[cur ^ 1] = 0;
       c->touched[(level + 1) & 1] = 0;
     }
-    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+    mark(kPhClear);
+    if (!barrier()) return;
 
     // Install the new frontier from the vertices that received bits.
     const int64_t T = (int64_t)__ldcg(touched);
@@ -453,7 +482,8 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         }
       }
     }
-    if (!grid_barrier(c, nblocks, a.limit_ns)) return;
+    mark(kPhInstall);
+    if (!barrier()) return;
     cur ^= 1;
     if (tid == 0) {
       c->levels = level;
@@ -464,6 +494,8 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
     }
   }
   if (tid == 0) c->t_end = globaltimer();
+  __syncthreads();
+  if (threadIdx.x < kMsPhases) atomicAdd(&c->phase_cycles[threadIdx.x], ph_acc[threadIdx.x]);
 }
 
 }  // namespace gbbfs

@@ -78,7 +78,13 @@ class MsStats(ctypes.Structure):
                 ("levels", ctypes.c_int32), ("lanes", ctypes.c_int32),
                 ("batch", ctypes.c_int32), ("alpha", ctypes.c_int32),
                 ("td_levels", ctypes.c_int32), ("bu_levels", ctypes.c_int32),
-                ("pad", ctypes.c_int32), ("td_ms", ctypes.c_double), ("bu_ms", ctypes.c_double)]
+                ("pad", ctypes.c_int32), ("td_ms", ctypes.c_double), ("bu_ms", ctypes.c_double),
+                ("phase_share", ctypes.c_double * 8)]
+
+    PHASES = ("top_down", "bu_small", "bu_mid", "write", "hub", "clear", "install", "barrier")
+
+    def phases(self):
+        return {k: round(self.phase_share[i], 4) for i, k in enumerate(self.PHASES)}
 
 
 _lib = None

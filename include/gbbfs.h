@@ -153,6 +153,10 @@ typedef struct gbbfs_ms_stats {
   int32_t td_levels, bu_levels; /* levels run top-down / bottom-up (all batches) */
   int32_t pad;
   double td_ms, bu_ms;          /* device time spent in them            */
+  /* share of warp time per kernel phase: top-down expansion, bottom-up
+   * small-vertex stream, bottom-up per-vertex scans, depth writes and
+   * queueing, hub chunks, frontier clear, frontier install, grid barriers */
+  double phase_share[8];
 } gbbfs_ms_stats;
 
 /* BFS depths from k sources.  depth_out (host) receives k rows of n entries,
