@@ -34,9 +34,9 @@ struct MsState {
   int depth_bytes = 0;
   int lanes = 0;
   void* visit = nullptr;
-  void* fr = nullptr;
+  void* fr[2] = {nullptr, nullptr};
   void* acc = nullptr;
-  uint32_t* fbits = nullptr;
+  uint32_t* fbits[2] = {nullptr, nullptr};
   int32_t* q[2] = {nullptr, nullptr};
   uint32_t* qc[2] = {nullptr, nullptr};
   int32_t* tq = nullptr;
@@ -75,9 +75,11 @@ void msbfs_release(MsState* ms) {
     if (ms->copied[i]) cudaEventDestroy(ms->copied[i]);
   }
   cudaFree(ms->visit);
-  cudaFree(ms->fr);
+  cudaFree(ms->fr[0]);
+  cudaFree(ms->fr[1]);
   cudaFree(ms->acc);
-  cudaFree(ms->fbits);
+  cudaFree(ms->fbits[0]);
+  cudaFree(ms->fbits[1]);
   cudaFree(ms->tq);
   cudaFree(ms->hubs);
   cudaFree(ms->hub_chunk);
@@ -92,11 +94,12 @@ void msbfs_release(MsState* ms) {
 // ---------------------------------------------------------------------------
 // Host side.
 
-// Lane words are allocated at 64 bits so both lane widths fit: visit, fr,
-// acc; queues q0/q1, chunk prefixes qc0/qc1 and tq; the frontier union; two
-// depth buffers of 64 rows; slack for the hub list and control blocks.
+// Lane words are allocated at 64 bits so both lane widths fit: visit, the
+// two frontier buffers, acc; queues q0/q1, chunk prefixes qc0/qc1 and tq; two
+// frontier unions; two depth buffers of 64 rows; slack for the hub list and
+// control blocks.
 size_t ms_state_bytes(int64_t n, int64_t W, int depth_bytes) {
-  return 3 * 8 * (size_t)n + 5 * 4 * (size_t)n + 4 * (size_t)W +
+  return 4 * 8 * (size_t)n + 5 * 4 * (size_t)n + 8 * (size_t)W +
          2 * (size_t)64 * n * depth_bytes + (16 << 20);
 }
 
@@ -168,9 +171,11 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
     return GBBFS_OK;
   };
   GB_TRY(alloc(&ms->visit, 8 * (size_t)n));
-  GB_TRY(alloc(&ms->fr, 8 * (size_t)n));
+  GB_TRY(alloc(&ms->fr[0], 8 * (size_t)n));
+  GB_TRY(alloc(&ms->fr[1], 8 * (size_t)n));
   GB_TRY(alloc(&ms->acc, 8 * (size_t)n));
-  GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits), 4 * (size_t)g->W));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[0]), 4 * (size_t)g->W));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[1]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
   // Hubs (degree above kMsHubDeg) and the prefix of their work chunks.
   ms->nhubs = (int64_t)g->hubs.size();
@@ -198,8 +203,9 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   GB_CUDA(cudaStreamCreateWithFlags(&ms->copy_stream, cudaStreamNonBlocking));
   GB_CUDA(cudaEventCreate(&ms->ev0));
   GB_CUDA(cudaEventCreate(&ms->ev1));
-  // visit / fr / acc start (and are left) all-zero between batches: every
-  // batch clears them in its own graph before the kernel runs.
+  // Every batch's graph clears visit, acc, the level-1 frontier buffers and
+  // the control block before the kernel runs; the other frontier buffers are
+  // cleared or written densely by the kernel itself.
   return GBBFS_OK;
 }
 
@@ -221,10 +227,12 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.n = g->n;
   a.m = g->m;
   a.visit = reinterpret_cast<LaneT*>(ms->visit);
-  a.fr = reinterpret_cast<LaneT*>(ms->fr);
+  a.fr0 = reinterpret_cast<LaneT*>(ms->fr[0]);
+  a.fr1 = reinterpret_cast<LaneT*>(ms->fr[1]);
   a.acc = reinterpret_cast<LaneT*>(ms->acc);
   a.W = g->W;
-  a.fbits = ms->fbits;
+  a.fbits0 = ms->fbits[0];
+  a.fbits1 = ms->fbits[1];
   a.q0 = ms->q[0];
   a.q1 = ms->q[1];
   a.qc0 = ms->qc[0];
@@ -247,9 +255,9 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   cudaError_t e = cudaMemcpyAsync(ms->d_src[buf], ms->h_src + 64 * buf, 64 * sizeof(int32_t),
                                   cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->visit, 0, lane_bytes, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr, 0, lane_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr[1], 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->acc, 0, lane_bytes, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ms->fbits, 0, 4 * (size_t)g->W, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->fbits[1], 0, 4 * (size_t)g->W, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->ctl[buf], 0, sizeof(MsCtl), s);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(ms->depth[buf], 0xff, (size_t)k * g->n * sizeof(DepthT), s);

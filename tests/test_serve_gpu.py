@@ -97,7 +97,7 @@ def test_admission_budget(native, pool):
     n_of = [g.n for _, g in pool]
     biggest = max(g.n for _, g in pool)
     W = (biggest + 31) // 32
-    budget = 3 * 8 * biggest + 5 * 4 * biggest + 4 * W + 2 * 64 * biggest + (16 << 20)
+    budget = 4 * 8 * biggest + 5 * 4 * biggest + 8 * W + 2 * 64 * biggest + (16 << 20)
     with native.Server(mode=0, hbm_budget_bytes=budget) as srv:
         for _, g in pool:
             srv.add_graph(g)
