@@ -38,7 +38,7 @@ struct MsState {
   void* acc = nullptr;
   uint32_t* fbits[2] = {nullptr, nullptr};
   int32_t* q[2] = {nullptr, nullptr};
-  uint32_t* qc[2] = {nullptr, nullptr};
+  uint64_t* qe[2] = {nullptr, nullptr};
   int32_t* tq = nullptr;
   int32_t* hubs = nullptr;
   uint32_t* hub_chunk = nullptr;
@@ -67,7 +67,7 @@ void msbfs_release(MsState* ms) {
   for (int i = 0; i < 2; i++) {
     if (ms->exec[i]) cudaGraphExecDestroy(ms->exec[i]);
     cudaFree(ms->q[i]);
-    cudaFree(ms->qc[i]);
+    cudaFree(ms->qe[i]);
     cudaFree(ms->depth[i]);
     cudaFree(ms->d_src[i]);
     cudaFree(ms->ctl[i]);
@@ -95,11 +95,11 @@ void msbfs_release(MsState* ms) {
 // Host side.
 
 // Lane words are allocated at 64 bits so both lane widths fit: visit, the
-// two frontier buffers, acc; queues q0/q1, chunk prefixes qc0/qc1 and tq; two
-// frontier unions; two depth buffers of 64 rows; slack for the hub list and
-// control blocks.
+// two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
+// and tq; two frontier unions; two depth buffers of 64 rows; slack for the
+// hub list and control blocks.
 size_t ms_state_bytes(int64_t n, int64_t W, int depth_bytes) {
-  return 4 * 8 * (size_t)n + 5 * 4 * (size_t)n + 8 * (size_t)W +
+  return 4 * 8 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 8 * (size_t)W +
          2 * (size_t)64 * n * depth_bytes + (16 << 20);
 }
 
@@ -189,7 +189,7 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   }
   for (int i = 0; i < 2; i++) {
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->q[i]), 4 * (size_t)n));
-    GB_TRY(alloc(reinterpret_cast<void**>(&ms->qc[i]), 4 * (size_t)n));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->qe[i]), 8 * (size_t)n));
     GB_TRY(alloc(&ms->depth[i], (size_t)64 * n * depth_bytes));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), 64 * sizeof(int32_t)));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->ctl[i]), sizeof(MsCtl)));
@@ -235,8 +235,8 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.fbits1 = ms->fbits[1];
   a.q0 = ms->q[0];
   a.q1 = ms->q[1];
-  a.qc0 = ms->qc[0];
-  a.qc1 = ms->qc[1];
+  a.qe0 = ms->qe[0];
+  a.qe1 = ms->qe[1];
   a.tq = ms->tq;
   a.hubs = ms->hubs;
   a.hub_chunk = ms->hub_chunk;
@@ -344,6 +344,8 @@ struct MsTally {
   int td_levels = 0, bu_levels = 0;
   double td_ms = 0, bu_ms = 0;
   double phase[kMsPhases] = {};
+  double level_ms[32] = {}, level_f[32] = {}, level_e[32] = {};
+  int level_bu[32] = {};
 };
 
 int check_batch(gbbfs_graph* g, int buf, MsTally* t) {
@@ -361,6 +363,12 @@ int check_batch(gbbfs_graph* g, int buf, MsTally* t) {
     t->levels = std::max(t->levels, c.levels);
     for (int l = 1; l <= c.levels && l < kMsTimedLevels; l++) {
       const double ms_l = (double)(c.level_end[l] - c.level_end[l - 1]) * 1e-6;
+      if (l < 32) {
+        t->level_ms[l] += ms_l;
+        t->level_f[l] += (double)c.level_f[l];
+        t->level_e[l] += (double)c.level_e[l];
+        t->level_bu[l] += c.level_bu[l];
+      }
       if (c.level_bu[l]) {
         t->bu_ms += ms_l;
         t->bu_levels++;
@@ -428,6 +436,12 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
     for (int p = 0; p < kMsPhases; p++) total += tally.phase[p];
     for (int p = 0; p < kMsPhases && p < 8; p++)
       st->phase_share[p] = total > 0 ? tally.phase[p] / total : 0.0;
+    for (int l = 0; l < 32; l++) {
+      st->level_ms[l] = tally.level_ms[l];
+      st->level_frontier[l] = tally.level_f[l];
+      st->level_edges[l] = tally.level_e[l];
+      st->level_bu[l] = tally.level_bu[l];
+    }
   }
   return GBBFS_OK;
 }
@@ -509,6 +523,11 @@ int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg) {
   cfg->batch = c.batch;
   cfg->alpha = c.alpha;
   return GBBFS_OK;
+}
+
+int64_t gbbfs_msbfs_state_bytes(int64_t n, int depth_bytes) {
+  if (n < 0 || (depth_bytes != 1 && depth_bytes != 4)) return -1;
+  return (int64_t)gbbfs::ms_state_bytes(n, (n + 31) / 32, depth_bytes);
 }
 
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,

@@ -8,25 +8,30 @@
 //                       before fr[v] is read, so neighbours outside every
 //                       frontier cost one L2-resident bit instead of a word
 //   acc        L[n]     bits merged by atomics (top-down levels and hubs)
-//   q0/q1      int32    top-down queue of a frontier and qc0/qc1, the first
-//                       work chunk of each entry
+//   q0/q1      int32    top-down queue of a frontier (vertices with edges) and
+//   qe0/qe1    u64      the position of each entry's first edge in the
+//                       concatenated adjacency of the queue
 //   tq         int32    vertices whose acc received bits in this level
 //   hubs       int32    vertices of degree > kMsHubDeg, with their chunk prefix
 //   depth      D[k][n]  per-source depth, [source][vertex] order
 //
 // One persistent cooperative kernel runs all levels of a batch.  Level l
 // reads the frontier in fr[l & 1] and writes the next one to fr[(l+1) & 1]:
-//   top-down (frontier summed degree <= m / alpha): the next buffer is
-//     cleared densely; a warp per kMsTdChunk-edge work item of a queued
-//     frontier vertex ORs fr[u] & ~visit[v] into acc[v] (atomicOr) and queues
-//     first touches; after a grid barrier every touched vertex is installed
-//     (visit, depth, next frontier, next queue).  The queue of a frontier
-//     that a bottom-up level produced is first compacted from its fbits.
-//   bottom-up: a warp per 32 consecutive vertices.  The concatenated
-//     adjacency of the tile's unfinished vertices of degree up to kMsSmall is
-//     streamed 32 edges per lane-step into per-vertex words in shared
-//     memory; vertices up to kMsHubDeg get the whole warp with early exit
-//     once every lane is found.  The warp then writes visit, the depth rows
+//   top-down (frontier summed degree <= m / alpha): warps take spans of
+//     kMsTdSpan consecutive edges of the queue's concatenated adjacency and
+//     OR fr[u] & ~visit[v] into acc[v] (atomicOr).  After a grid barrier the
+//     next frontier is installed (visit, depth, next frontier words): for a
+//     frontier with few edges from a list of first touches into a cleared
+//     buffer, queueing the vertices as they are installed; for one with
+//     more than n/16 edges by a pass over all vertices that writes every
+//     word.  A frontier that was written densely is queued from its fbits
+//     when a top-down level needs it.
+//   bottom-up: a warp per tile of 32 consecutive vertices, tiles handed out
+//     kMsGrab at a time from a counter.  The concatenated adjacency of the
+//     tile's unfinished vertices of degree below kMsSmall is streamed 32
+//     edges per lane-step into per-vertex words in shared memory; vertices
+//     up to kMsHubDeg get the whole warp with early exit once every lane is
+//     found.  The warp then writes visit, the depth rows
 //     (coalesced per source), the next frontier words and their fbits word
 //     densely, so no clear or install pass follows.  Hub adjacency is cut
 //     into kMsHubChunk-edge items merged into acc and installed after the
@@ -45,16 +50,18 @@ enum MsPhase {
   kPhTopDown = 0, kPhSmall, kPhMid, kPhWrite, kPhHub, kPhClear, kPhInstall, kPhBarrier,
   kMsPhases
 };
-constexpr int kMsSmall = 256;
+constexpr int kMsSmall = 32;        // bottom-up: lower degrees share a streamed pass
+constexpr int kMsGrab = 8;          // tiles of 32 vertices a warp takes at a time
 constexpr int kMsHubDeg = 2048;
 constexpr int kMsHubChunk = 2048;
-constexpr int kMsTdChunk = 1024;
+constexpr int kMsTdSpan = 2048;     // edges per warp span of a top-down level
 
 struct MsCtl {
   unsigned long long q_packed[2];   // top-down queue q[i]: (count << shift) | chunks
   unsigned long long f_count[3];    // frontier of level l: vertices (slot l % 3)
   unsigned long long f_edges[3];    //   and their summed degree
   unsigned long long touched[3];    // tq entries of level l (slot l % 3)
+  unsigned long long tile_next[3];  // next bottom-up tile of level l (slot l % 3)
   unsigned int bar_count;
   unsigned int bar_gen;
   int error;
@@ -62,6 +69,8 @@ struct MsCtl {
   unsigned long long t_begin, t_end;
   unsigned long long level_end[kMsTimedLevels];   // %globaltimer at the end of each level
   int level_bu[kMsTimedLevels];                    // 1 when the level ran bottom-up
+  unsigned long long level_f[kMsTimedLevels];      // frontier vertices of each level
+  unsigned long long level_e[kMsTimedLevels];      //   and their summed degree
   unsigned long long phase_cycles[kMsPhases];      // SM cycles per phase, summed over warps
 };
 
@@ -78,8 +87,8 @@ struct MsArgs {
   uint32_t* fbits1;
   int32_t* q0;
   int32_t* q1;
-  uint32_t* qc0;
-  uint32_t* qc1;
+  uint64_t* qe0;   // first edge of each queue entry in the queue's concatenated adjacency
+  uint64_t* qe1;
   int32_t* tq;
   const int32_t* hubs;
   const uint32_t* hub_chunk;   // nhubs + 1 entries
@@ -124,8 +133,16 @@ __device__ __forceinline__ int lowest_bit(LaneT x) {
     return __ffs((int)x) - 1;
 }
 
+// Frontier words and bits are read with L1-cached loads: they are written
+// only in the level before, and the acquire fence of the grid barrier in
+// between makes those writes visible to the weak loads after it.
+template <typename LaneT>
+__device__ __forceinline__ LaneT ld_frontier(const LaneT* p) {
+  return *p;
+}
+
 __device__ __forceinline__ bool in_frontier(const uint32_t* fbits, int32_t u) {
-  return (__ldcg(fbits + (u >> 5)) >> (u & 31)) & 1u;
+  return (fbits[u >> 5] >> (u & 31)) & 1u;
 }
 
 // Grid-wide barrier with a time bound.  Returns false (and every later call
@@ -167,14 +184,33 @@ __device__ __forceinline__ bool grid_barrier(MsCtl* c, unsigned nblocks,
 
 // Depth `level` for every source bit of `nb` at vertex v.  Called by a whole
 // warp; lanes with consecutive v write consecutive entries of each row.
+// Rows are visited one 32-bit half of the lane word at a time: a half with
+// many rows set runs every row unrolled, a sparse one only its set rows.
 template <typename LaneT, typename DepthT>
 __device__ __forceinline__ void write_depths(DepthT* depth, int64_t n, int64_t v, LaneT nb,
                                              int level) {
-  LaneT any = warp_or(nb);
-  while (any) {
-    const int i = lowest_bit(any);
-    any &= any - 1;
-    if ((nb >> i) & 1) depth[(int64_t)i * n + v] = (DepthT)level;
+  const LaneT any = warp_or(nb);
+  const DepthT d = (DepthT)level;
+#pragma unroll
+  for (int h = 0; h < (int)(sizeof(LaneT) / 4); h++) {
+    unsigned anyh = (unsigned)((unsigned long long)any >> (32 * h));
+    if (!anyh) continue;
+    unsigned bits = (unsigned)((unsigned long long)nb >> (32 * h));
+    DepthT* p = depth + (int64_t)(32 * h) * n + v;
+    if (__popc(anyh) > 12) {
+#pragma unroll 8
+      for (int i = 0; i < 32; i++) {
+        if (bits & 1u) *p = d;
+        bits >>= 1;
+        p += n;
+      }
+    } else {
+      while (anyh) {
+        const int i = __ffs(anyh) - 1;
+        anyh &= anyh - 1;
+        if ((bits >> i) & 1u) p[(int64_t)i * n] = d;
+      }
+    }
   }
 }
 
@@ -191,33 +227,44 @@ __device__ __forceinline__ void warp_append(unsigned long long* counter, int32_t
   }
 }
 
-// Append the lanes with `keep` to a top-down queue with its work-chunk
-// prefix, and add them to the frontier totals.  Whole warp.
-__device__ __forceinline__ void warp_enqueue(unsigned long long* packed, int32_t* q, uint32_t* qc,
+// Append the lanes with `keep` and a non-empty adjacency to a top-down queue.
+// The packed counter is (entries << shift) | summed degree, so one atomic
+// gives each entry its slot and the position of its first edge in the
+// concatenated adjacency of the queue (qe).  Whole warp.
+__device__ __forceinline__ void warp_queue(unsigned long long* packed, int32_t* q, uint64_t* qe,
+                                           int shift, bool keep, int32_t v,
+                                           unsigned long long deg) {
+  const int lane = threadIdx.x & 31;
+  keep = keep && deg > 0;
+  if (!__any_sync(kFull, keep)) return;
+  const unsigned long long emask = (1ull << shift) - 1;
+  const unsigned long long mine = keep ? (1ull << shift) + deg : 0;
+  const unsigned long long inc = warp_inclusive_sum(mine, lane);
+  unsigned long long base = 0;
+  if (lane == 31) base = atomicAdd(packed, inc);
+  base = shfl(base, 31);
+  if (keep) {
+    const unsigned long long at = base + inc - mine;
+    q[at >> shift] = v;
+    qe[at >> shift] = at & emask;
+  }
+}
+
+// warp_queue, and the lanes with `keep` added to the frontier totals.
+__device__ __forceinline__ void warp_enqueue(unsigned long long* packed, int32_t* q, uint64_t* qe,
                                              unsigned long long* f_count,
                                              unsigned long long* f_edges, int shift, bool keep,
                                              int32_t v, unsigned long long deg) {
   const int lane = threadIdx.x & 31;
   const unsigned km = __ballot_sync(kFull, keep);
   if (!km) return;
-  const unsigned long long emask = (1ull << shift) - 1;
-  const unsigned long long chunks = keep ? (deg + kMsTdChunk - 1) / kMsTdChunk : 0;
-  const unsigned long long mine = keep ? (1ull << shift) + chunks : 0;
-  const unsigned long long inc = warp_inclusive_sum(mine, lane);
+  warp_queue(packed, q, qe, shift, keep, v, deg);
   unsigned long long dsum = keep ? deg : 0;
 #pragma unroll
   for (int o = 16; o; o >>= 1) dsum += __shfl_xor_sync(kFull, dsum, o);
-  unsigned long long base = 0;
-  if (lane == 31) {
-    base = atomicAdd(packed, inc);
+  if (lane == 0) {
     atomicAdd(f_count, (unsigned long long)__popc(km));
     atomicAdd(f_edges, dsum);
-  }
-  base = shfl(base, 31);
-  if (keep) {
-    const unsigned long long at = base + inc - mine;
-    q[at >> shift] = v;
-    qc[at >> shift] = (uint32_t)(at & emask);
   }
 }
 
@@ -227,7 +274,7 @@ __device__ __forceinline__ void warp_enqueue(unsigned long long* packed, int32_t
 template <typename LaneT>
 __device__ __forceinline__ LaneT warp_gather_or(const int32_t* nbr, const uint32_t* fbits,
                                                 const LaneT* fr, uint64_t b, uint64_t e,
-                                                LaneT vis, LaneT all) {
+                                                LaneT vis, LaneT all, bool filter) {
   const int lane = threadIdx.x & 31;
   LaneT got = 0;
   for (uint64_t e0 = b; e0 < e; e0 += 128) {
@@ -239,20 +286,27 @@ __device__ __forceinline__ LaneT warp_gather_or(const int32_t* nbr, const uint32
     }
     bool in[4];
 #pragma unroll
-    for (int r = 0; r < 4; r++) in[r] = u[r] >= 0 && in_frontier(fbits, u[r]);
+    for (int r = 0; r < 4; r++) in[r] = u[r] >= 0 && (!filter || in_frontier(fbits, u[r]));
     LaneT x = 0;
 #pragma unroll
     for (int r = 0; r < 4; r++)
-      if (in[r]) x |= ld_lane(fr + u[r]);
+      if (in[r]) x |= ld_frontier(fr + u[r]);
     got |= warp_or(x);
     if (((got | vis) & all) == all) break;
   }
   return got;
 }
 
+// Resident blocks per SM the register allocation is held to.
+#ifndef GBBFS_MS_MIN_BLOCKS
+#define GBBFS_MS_MIN_BLOCKS 4
+#endif
+
 template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
-__global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
+__global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
   __shared__ LaneT tile_acc[kWarpsPerCta][32];
+  __shared__ int64_t tile_base[kWarpsPerCta][32];
+  __shared__ uint8_t tile_owner[kWarpsPerCta][32 * kMsSmall];
   __shared__ unsigned long long blk_count, blk_edges;
   __shared__ unsigned long long ph_acc[kMsPhases];
   MsCtl* c = a.ctl;
@@ -295,10 +349,11 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
     a.depth[(int64_t)i * a.n + s] = 0;
     if (atomic_or_lane(a.fr1 + s, bit) == 0) {
       const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
-      const unsigned long long chunks = (deg + kMsTdChunk - 1) / kMsTdChunk;
-      const unsigned long long at = atomicAdd(&c->q_packed[1], (1ull << a.shift) + chunks);
-      a.q1[at >> a.shift] = s;
-      a.qc1[at >> a.shift] = (uint32_t)(at & emask);
+      if (deg) {
+        const unsigned long long at = atomicAdd(&c->q_packed[1], (1ull << a.shift) + deg);
+        a.q1[at >> a.shift] = s;
+        a.qe1[at >> a.shift] = at & emask;
+      }
       atomicAdd(&c->f_count[1], 1ull);
       atomicAdd(&c->f_edges[1], deg);
       atomicOr(a.fbits1 + (s >> 5), 1u << (s & 31));
@@ -322,9 +377,9 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
     const uint32_t* fb = cur ? a.fbits1 : a.fbits0;
     uint32_t* fbn = cur ? a.fbits0 : a.fbits1;
     int32_t* q = cur ? a.q1 : a.q0;
-    uint32_t* qc = cur ? a.qc1 : a.qc0;
+    uint64_t* qe = cur ? a.qe1 : a.qe0;
     int32_t* qn = cur ? a.q0 : a.q1;
-    uint32_t* qcn = cur ? a.qc0 : a.qc1;
+    uint64_t* qen = cur ? a.qe0 : a.qe1;
     unsigned long long* touched = &c->touched[level % 3];
     unsigned long long* nf_count = &c->f_count[(level + 1) % 3];
     unsigned long long* nf_edges = &c->f_edges[(level + 1) % 3];
@@ -334,13 +389,17 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
       c->f_count[(level + 2) % 3] = 0;
       c->f_edges[(level + 2) % 3] = 0;
       c->touched[(level + 2) % 3] = 0;
+      c->tile_next[(level + 2) % 3] = 0;
       c->q_packed[nxt] = 0;
     }
 
     if (!bottom_up) {
+      // A frontier with many edges reaches many vertices: install the next
+      // frontier by one pass over all vertices instead of a touched list.
+      const bool dense = E > (unsigned long long)(a.n >> 4);
       if (!have_queue) {
-        // The frontier came from a bottom-up level: queue it from its fbits.
-        // (q_packed[cur] was reset by the previous level.)
+        // The frontier was written densely (bottom-up or dense install):
+        // queue it from its fbits.  (q_packed[cur] was reset a level ago.)
         for (int64_t w0 = warp << 5; w0 < a.W; w0 += nwarps << 5) {
           const int64_t w = w0 + lane;
           uint32_t bits = w < a.W ? __ldcg(fb + w) : 0u;
@@ -353,88 +412,168 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
               bits &= bits - 1;
               deg = (unsigned long long)(a.off[v + 1] - a.off[v]);
             }
-            const unsigned long long chunks = keep ? (deg + kMsTdChunk - 1) / kMsTdChunk : 0;
-            const unsigned long long mine = keep ? (1ull << a.shift) + chunks : 0;
-            const unsigned long long inc = warp_inclusive_sum(mine, lane);
-            unsigned long long base = 0;
-            if (lane == 31) base = atomicAdd(&c->q_packed[cur], inc);
-            base = shfl(base, 31);
-            if (keep) {
-              const unsigned long long at = base + inc - mine;
-              q[at >> a.shift] = v;
-              qc[at >> a.shift] = (uint32_t)(at & emask);
-            }
+            warp_queue(&c->q_packed[cur], q, qe, a.shift, keep, v, deg);
           }
         }
         mark(kPhInstall);
         if (!barrier()) return;
       }
       const unsigned long long qp = __ldcg(&c->q_packed[cur]);
-      const int64_t C = (int64_t)(qp & emask);
+      const uint64_t EQ = qp & emask;             // edges of the queued vertices
       const int64_t Q = (int64_t)(qp >> a.shift);
-      // The next frontier buffers are written sparsely: clear them first.
-      for (int64_t v = tid; v < a.n; v += nthreads) frn[v] = 0;
-      for (int64_t w = tid; w < a.W; w += nthreads) fbn[w] = 0;
-      mark(kPhClear);
-      // Top-down: a warp per work chunk of one frontier vertex.
-      for (int64_t ch = warp; ch < C; ch += nwarps) {
+      if (!dense) {
+        // The next frontier buffers are written sparsely: clear them first.
+        for (int64_t v = tid; v < a.n; v += nthreads) frn[v] = 0;
+        for (int64_t w = tid; w < a.W; w += nthreads) fbn[w] = 0;
+        mark(kPhClear);
+      }
+      // Top-down, edge-balanced: warp spans of consecutive edges of
+      // the queue's concatenated adjacency.  Lane j of the warp holds queue
+      // entry base + j (its first edge, adjacency start and frontier word);
+      // the window slides so that entry `base` holds the round's first edge,
+      // and since every entry has an edge, the round's 32 edges lie in the
+      // window.
+      // Spans shrink (to 32 edges at least) until every warp has one.
+      uint64_t span = (EQ + nwarps - 1) / nwarps;
+      span = span < 32 ? 32 : span > kMsTdSpan ? kMsTdSpan : (span + 31) & ~31ull;
+      const int64_t nspans = (int64_t)((EQ + span - 1) / span);
+      for (int64_t sp = warp; sp < nspans; sp += nwarps) {
+        const uint64_t e_lo = (uint64_t)sp * span;
+        const uint64_t e_hi = e_lo + span < EQ ? e_lo + span : EQ;
         int64_t lo = 0, hi = Q - 1;
         while (lo < hi) {
           const int64_t mid = (lo + hi + 1) >> 1;
-          if ((int64_t)qc[mid] <= ch) lo = mid; else hi = mid - 1;
+          if (__ldcg(qe + mid) <= e_lo) lo = mid; else hi = mid - 1;
         }
-        const int32_t u = q[lo];
-        const LaneT f = ld_lane(fr + u);
-        const uint64_t b = (uint64_t)a.off[u] + (uint64_t)(ch - qc[lo]) * kMsTdChunk;
-        const uint64_t ue = (uint64_t)a.off[u + 1];
-        const uint64_t e = b + kMsTdChunk < ue ? b + kMsTdChunk : ue;
-        for (uint64_t e0 = b; e0 < e; e0 += 128) {
-          int32_t v[4];
-          LaneT vis[4];
-#pragma unroll
-          for (int r = 0; r < 4; r++) {
-            const uint64_t idx = e0 + 32 * r + lane;
-            v[r] = idx < e ? __ldg(a.nbr + idx) : -1;
+        int64_t base = lo;
+        uint64_t pre = ~0ull, ob = 0;
+        LaneT f = 0;
+        auto load_entry = [&](int64_t j) {
+          if (j < Q) {
+            pre = __ldcg(qe + j);
+            const int32_t u = __ldcg(q + j);
+            ob = (uint64_t)a.off[u];
+            f = ld_frontier(fr + u);
+          } else {
+            pre = ~0ull;
+            ob = 0;
+            f = 0;
           }
-#pragma unroll
-          for (int r = 0; r < 4; r++) vis[r] = v[r] >= 0 ? ld_lane(a.visit + v[r]) : all;
-          bool first[4];
-#pragma unroll
-          for (int r = 0; r < 4; r++) {
-            const LaneT nb = f & ~vis[r];
-            first[r] = v[r] >= 0 && nb && atomic_or_lane(a.acc + v[r], nb) == 0;
+        };
+        load_entry(base + lane);
+        for (uint64_t e0 = e_lo; e0 < e_hi; e0 += 32) {
+          for (;;) {
+            const unsigned le = __ballot_sync(kFull, pre <= e0);
+            const int s = 31 - __clz(le);
+            if (s <= 0) break;
+            const int src = lane + s;
+            const uint64_t pre2 = shfl(pre, src & 31), ob2 = shfl(ob, src & 31);
+            const LaneT f2 = shfl(f, src & 31);
+            if (src < 32) {
+              pre = pre2;
+              ob = ob2;
+              f = f2;
+            } else {
+              load_entry(base + src);
+            }
+            base += s;
           }
+          const uint64_t e = e0 + lane;
+          int seg = 0;
 #pragma unroll
-          for (int r = 0; r < 4; r++) warp_append(touched, a.tq, first[r], v[r]);
+          for (int step = 16; step; step >>= 1)
+            if (shfl(pre, seg + step) <= e) seg += step;
+          const uint64_t pre_s = shfl(pre, seg), ob_s = shfl(ob, seg);
+          const LaneT f_s = shfl(f, seg);
+          bool first = false;
+          int32_t v = 0;
+          if (e < e_hi) {
+            v = __ldg(a.nbr + ob_s + (e - pre_s));
+            if (dense) {
+              // No visit test: the install pass masks visited bits anyway,
+              // and the OR needs no result, so nothing waits on a load.
+              atomic_or_lane(a.acc + v, f_s);
+            } else {
+              const LaneT nb = f_s & ~ld_lane(a.visit + v);
+              if (nb) first = atomic_or_lane(a.acc + v, nb) == 0;
+            }
+          }
+          if (!dense) warp_append(touched, a.tq, first, v);
         }
       }
       mark(kPhTopDown);
       if (!barrier()) return;
-      // Install every touched vertex.
-      const int64_t T = (int64_t)__ldcg(touched);
-      for (int64_t i0 = warp << 5; i0 < T; i0 += nwarps << 5) {
-        const int64_t i = i0 + lane;
-        int32_t v = 0;
-        LaneT nb = 0;
-        unsigned long long deg = 0;
-        if (i < T) {
-          v = a.tq[i];
-          nb = a.acc[v];
-          a.acc[v] = 0;
-          const LaneT vis = a.visit[v];
-          nb &= ~vis;
-          if (nb) {
-            a.visit[v] = vis | nb;
-            for (LaneT x = nb; x; x &= x - 1)
-              a.depth[(int64_t)lowest_bit(x) * a.n + v] = (DepthT)level;
-            frn[v] = nb;
-            atomicOr(fbn + (v >> 5), 1u << (v & 31));
-            deg = (unsigned long long)(a.off[v + 1] - a.off[v]);
-          }
+      if (dense) {
+        // Every vertex: bits that arrived and were not yet visited.
+        if (threadIdx.x == 0) {
+          blk_count = 0;
+          blk_edges = 0;
         }
-        warp_enqueue(&c->q_packed[nxt], qn, qcn, nf_count, nf_edges, a.shift, nb != 0, v, deg);
+        __syncthreads();
+        unsigned long long my_count = 0, my_edges = 0;
+        for (int64_t v0 = warp << 5; v0 < a.n; v0 += nwarps << 5) {
+          const int64_t v = v0 + lane;
+          LaneT nb = 0;
+          if (v < a.n) {
+            const LaneT x = ld_lane(a.acc + v);
+            if (x) {
+              a.acc[v] = 0;
+              const LaneT vis = a.visit[v];
+              nb = x & ~vis;
+              if (nb) {
+                a.visit[v] = vis | nb;
+                my_count++;
+                my_edges += (unsigned long long)(a.off[v + 1] - a.off[v]);
+              }
+            }
+            frn[v] = nb;
+          }
+          const unsigned nm = __ballot_sync(kFull, nb != 0);
+          if (lane == 0) fbn[v0 >> 5] = nm;
+          write_depths(a.depth, a.n, v, nb, level);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          my_count += __shfl_xor_sync(kFull, my_count, o);
+          my_edges += __shfl_xor_sync(kFull, my_edges, o);
+        }
+        if (lane == 0) {
+          atomicAdd(&blk_count, my_count);
+          atomicAdd(&blk_edges, my_edges);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && blk_count) {
+          atomicAdd(nf_count, blk_count);
+          atomicAdd(nf_edges, blk_edges);
+        }
+        have_queue = false;
+      } else {
+        // Install every touched vertex.
+        const int64_t T = (int64_t)__ldcg(touched);
+        for (int64_t i0 = warp << 5; i0 < T; i0 += nwarps << 5) {
+          const int64_t i = i0 + lane;
+          int32_t v = 0;
+          LaneT nb = 0;
+          unsigned long long deg = 0;
+          if (i < T) {
+            v = a.tq[i];
+            nb = a.acc[v];
+            a.acc[v] = 0;
+            const LaneT vis = a.visit[v];
+            nb &= ~vis;
+            if (nb) {
+              a.visit[v] = vis | nb;
+              for (LaneT x = nb; x; x &= x - 1)
+                a.depth[(int64_t)lowest_bit(x) * a.n + v] = (DepthT)level;
+              frn[v] = nb;
+              atomicOr(fbn + (v >> 5), 1u << (v & 31));
+              deg = (unsigned long long)(a.off[v + 1] - a.off[v]);
+            }
+          }
+          warp_enqueue(&c->q_packed[nxt], qn, qen, nf_count, nf_edges, a.shift, nb != 0, v, deg);
+        }
+        have_queue = true;
       }
-      have_queue = true;
       mark(kPhInstall);
       if (!barrier()) return;
     } else {
@@ -445,7 +584,48 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
       }
       __syncthreads();
       unsigned long long my_count = 0, my_edges = 0;
-      for (int64_t v0 = warp << 5; v0 < a.n; v0 += nwarps << 5) {
+      const int wib = threadIdx.x >> 5;
+      uint8_t* own = tile_owner[wib];
+      int64_t* nbase = tile_base[wib];
+      LaneT* tacc = tile_acc[wib];
+      // When most edge endpoints are frontier vertices, the fbits test
+      // filters little and costs a load of its own: read fr[u] directly.
+      const bool filter = 2 * E < (unsigned long long)a.m;
+      const int64_t ngroups = (a.W + kMsGrab - 1) / kMsGrab;
+      unsigned long long* next_unit = &c->tile_next[level % 3];
+      for (;;) {
+        // Work units from a level-wide counter: the hub chunks first, then
+        // groups of kMsGrab tiles.
+        unsigned long long u0 = 0;
+        if (lane == 0) u0 = atomicAdd(next_unit, 1ull);
+        u0 = shfl(u0, 0);
+        if ((int64_t)u0 >= hub_chunks + ngroups) break;
+        if ((int64_t)u0 < hub_chunks) {
+          // A hub's adjacency cut into work items, merged by atomicOr.
+          const int64_t hc = (int64_t)u0;
+          int64_t lo = 0, hi = a.nhubs - 1;
+          while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if ((int64_t)a.hub_chunk[mid] <= hc) lo = mid; else hi = mid - 1;
+          }
+          const int32_t v = a.hubs[lo];
+          const LaneT vis = ld_lane(a.visit + v);
+          if ((vis & all) != all) {
+            const uint64_t b = (uint64_t)a.off[v] + (uint64_t)(hc - a.hub_chunk[lo]) * kMsHubChunk;
+            const uint64_t ve = (uint64_t)a.off[v + 1];
+            const uint64_t e = b + kMsHubChunk < ve ? b + kMsHubChunk : ve;
+            const LaneT got = warp_gather_or(a.nbr, fb, fr, b, e, vis, all, filter);
+            const LaneT part = got & ~vis & all;
+            bool first = false;
+            if (lane == 0 && part) first = atomic_or_lane(a.acc + v, part) == 0;
+            warp_append(touched, a.tq, first, v);
+          }
+          mark(kPhHub);
+          continue;
+        }
+        const int64_t v_begin = ((int64_t)u0 - hub_chunks) * (kMsGrab << 5);
+        const int64_t v_stop = v_begin + (kMsGrab << 5) < a.n ? v_begin + (kMsGrab << 5) : a.n;
+      for (int64_t v0 = v_begin; v0 < v_stop; v0 += 32) {
         const int64_t v = v0 + lane;
         LaneT vis = all;
         uint64_t b = 0, e = 0;
@@ -457,59 +637,59 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         const bool need = ((vis & all) != all) && e > b;
         const uint64_t deg = e - b;
         LaneT nb = 0;
-        // Small vertices: the warp streams their concatenated adjacency,
-        // kBatchN/2 x 32 edges per round, loads issued together; bits are
-        // ORed into per-vertex words in shared memory.
-        const bool small = need && deg <= (uint64_t)kMsSmall;
+        // Vertices of degree below kMsSmall: the warp streams their
+        // concatenated adjacency, kBatchN/2 x 32 edges per round with the
+        // loads of a round issued together.  own[t] names the tile lane that
+        // edge t of the stream belongs to; lanes of one owner combine their
+        // bits (match + warp reduction) and one of them ORs them into the
+        // owner's word in shared memory.
+        const bool small = need && deg < (uint64_t)kMsSmall;
         const unsigned sd = small ? (unsigned)deg : 0u;
         const unsigned sincl = warp_inclusive_sum(sd, lane);
         const unsigned sstart = sincl - sd;
         const unsigned stotal = __shfl_sync(kFull, sincl, 31);
-        LaneT* tacc = tile_acc[threadIdx.x >> 5];
         tacc[lane] = 0;
+        nbase[lane] = (int64_t)b - (int64_t)sstart;
+        for (unsigned t = sstart; t < sincl; t++) own[t] = (uint8_t)lane;
         __syncwarp();
         constexpr int kR = kBatchN / 2 > 0 ? kBatchN / 2 : 1;
         for (unsigned t0 = 0; t0 < stotal; t0 += 32 * kR) {
-          int seg[kR];
+          unsigned o[kR];
           int32_t u[kR];
 #pragma unroll
           for (int r = 0; r < kR; r++) {
             const unsigned t = t0 + 32 * r + lane;
-            const unsigned tc = t < stotal ? t : stotal - 1;
-            // last vertex of the tile whose stream starts at or before tc
-            // (every lane takes part in the shuffles)
-            int lo = 0;
-#pragma unroll
-            for (int step = 16; step; step >>= 1) {
-              const unsigned st = __shfl_sync(kFull, sstart, lo + step);
-              if (st <= tc) lo += step;
-            }
-            const uint64_t bs = shfl(b, lo);
-            const unsigned ss = __shfl_sync(kFull, sstart, lo);
-            seg[r] = t < stotal ? lo : -1;
-            u[r] = t < stotal ? __ldg(a.nbr + bs + (t - ss)) : -1;
+            o[r] = t < stotal ? own[t] : 32u;
+            u[r] = t < stotal ? __ldg(a.nbr + nbase[o[r]] + t) : -1;
           }
           bool in[kR];
 #pragma unroll
-          for (int r = 0; r < kR; r++) in[r] = u[r] >= 0 && in_frontier(fb, u[r]);
+          for (int r = 0; r < kR; r++) in[r] = u[r] >= 0 && (!filter || in_frontier(fb, u[r]));
 #pragma unroll
           for (int r = 0; r < kR; r++) {
-            if (in[r]) {
-              const LaneT x = ld_lane(fr + u[r]);
-              if (x) atomic_or_lane(tacc + seg[r], x);
+            const LaneT x = in[r] ? ld_frontier(fr + u[r]) : (LaneT)0;
+            const unsigned grp = __match_any_sync(kFull, o[r]);
+            LaneT red;
+            if constexpr (sizeof(LaneT) == 8) {
+              const unsigned lo = __reduce_or_sync(grp, (unsigned)x);
+              const unsigned hi = __reduce_or_sync(grp, (unsigned)((unsigned long long)x >> 32));
+              red = (LaneT)(((unsigned long long)hi << 32) | lo);
+            } else {
+              red = (LaneT)__reduce_or_sync(grp, (unsigned)x);
             }
+            if (o[r] < 32u && red && lane == __ffs(grp) - 1) tacc[o[r]] |= red;
           }
         }
         __syncwarp();
         if (small) nb = tacc[lane] & ~vis & all;
         mark(kPhSmall);
-        unsigned mids = __ballot_sync(kFull, need && deg > kMsSmall && deg <= kMsHubDeg);
+        unsigned mids = __ballot_sync(kFull, need && deg >= kMsSmall && deg <= kMsHubDeg);
         while (mids) {
           const int t = __ffs(mids) - 1;
           mids &= mids - 1;
           const LaneT vt = shfl(vis, t);
           const uint64_t bt = shfl(b, t), et = shfl(e, t);
-          const LaneT got = warp_gather_or(a.nbr, fb, fr, bt, et, vt, all);
+          const LaneT got = warp_gather_or(a.nbr, fb, fr, bt, et, vt, all, filter);
           if (lane == t) nb = got & ~vt & all;
         }
         mark(kPhMid);
@@ -525,26 +705,7 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
         }
         mark(kPhWrite);
       }
-      // Hubs: their adjacency cut into work items, merged by atomicOr.
-      for (int64_t hc = warp; hc < hub_chunks; hc += nwarps) {
-        int64_t lo = 0, hi = a.nhubs - 1;
-        while (lo < hi) {
-          const int64_t mid = (lo + hi + 1) >> 1;
-          if ((int64_t)a.hub_chunk[mid] <= hc) lo = mid; else hi = mid - 1;
-        }
-        const int32_t v = a.hubs[lo];
-        const LaneT vis = ld_lane(a.visit + v);
-        if ((vis & all) == all) continue;
-        const uint64_t b = (uint64_t)a.off[v] + (uint64_t)(hc - a.hub_chunk[lo]) * kMsHubChunk;
-        const uint64_t ve = (uint64_t)a.off[v + 1];
-        const uint64_t e = b + kMsHubChunk < ve ? b + kMsHubChunk : ve;
-        const LaneT got = warp_gather_or(a.nbr, fb, fr, b, e, vis, all);
-        const LaneT part = got & ~vis & all;
-        bool first = false;
-        if (lane == 0 && part) first = atomic_or_lane(a.acc + v, part) == 0;
-        warp_append(touched, a.tq, first, v);
       }
-      mark(kPhHub);
       // One pair of counter atomics per block.
 #pragma unroll
       for (int o = 16; o; o >>= 1) {
@@ -591,6 +752,8 @@ __global__ void __launch_bounds__(kThreads) k_msbfs(MsArgs<OffT, LaneT, DepthT> 
       if (level < kMsTimedLevels) {
         c->level_end[level] = globaltimer();
         c->level_bu[level] = bottom_up ? 1 : 0;
+        c->level_f[level] = (unsigned long long)F;
+        c->level_e[level] = E;
       }
     }
   }

@@ -33,7 +33,7 @@ EXPORTS = (
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
     "gbbfs_append_bfs_output", "gbbfs_msbfs", "gbbfs_msbfs_device", "gbbfs_msbfs_set_config",
-    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_server_open",
+    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_msbfs_state_bytes", "gbbfs_server_open",
     "gbbfs_server_add_graph", "gbbfs_server_submit", "gbbfs_server_poll", "gbbfs_server_drain",
     "gbbfs_server_clock", "gbbfs_server_close", "gbbfs_bfs_noalloc",
 )
@@ -79,12 +79,21 @@ class MsStats(ctypes.Structure):
                 ("batch", ctypes.c_int32), ("alpha", ctypes.c_int32),
                 ("td_levels", ctypes.c_int32), ("bu_levels", ctypes.c_int32),
                 ("pad", ctypes.c_int32), ("td_ms", ctypes.c_double), ("bu_ms", ctypes.c_double),
-                ("phase_share", ctypes.c_double * 8)]
+                ("phase_share", ctypes.c_double * 8),
+                ("level_ms", ctypes.c_double * 32), ("level_frontier", ctypes.c_double * 32),
+                ("level_edges", ctypes.c_double * 32), ("level_bu", ctypes.c_int32 * 32)]
 
     PHASES = ("top_down", "bu_small", "bu_mid", "write", "hub", "clear", "install", "barrier")
 
     def phases(self):
         return {k: round(self.phase_share[i], 4) for i, k in enumerate(self.PHASES)}
+
+    def per_level(self):
+        """[(level, ms, frontier vertices, frontier degree sum, bottom-up
+        batches)] summed over the batches of the call."""
+        top = min(self.levels, 31)
+        return [(l, self.level_ms[l], self.level_frontier[l], self.level_edges[l],
+                 self.level_bu[l]) for l in range(1, top + 1)]
 
 
 _lib = None
@@ -123,6 +132,7 @@ def lib():
             "gbbfs_msbfs_set_config": (I, [P, P]),
             "gbbfs_msbfs_get_config": (I, [P, P]),
             "gbbfs_msbfs_autotune": (I, [P, P, i64, I, P]),
+            "gbbfs_msbfs_state_bytes": (i64, [i64, I]),
             "gbbfs_server_open": (I, [P, PP]),
             "gbbfs_server_add_graph": (I, [P, P, P]),
             "gbbfs_server_submit": (I, [P, i32, i32, P, P]),
@@ -386,6 +396,14 @@ def msbfs_get_config(g):
     c = MsConfig()
     _check(lib().gbbfs_msbfs_get_config(g.handle, ctypes.byref(c)), "msbfs_get_config")
     return c.as_dict()
+
+
+def msbfs_state_bytes(n, depth_bytes=1):
+    """HBM bytes the batched search state of an n-vertex graph takes."""
+    r = lib().gbbfs_msbfs_state_bytes(int(n), int(depth_bytes))
+    if r < 0:
+        raise ValueError("bad arguments to msbfs_state_bytes")
+    return r
 
 
 def msbfs_autotune(g, sample, depth_bytes=1):

@@ -157,6 +157,12 @@ typedef struct gbbfs_ms_stats {
    * small-vertex stream, bottom-up per-vertex scans, depth writes and
    * queueing, hub chunks, frontier clear, frontier install, grid barriers */
   double phase_share[8];
+  /* per level l (1..31), summed over batches: device time, frontier
+   * vertices, their summed degree, and how many batches ran it bottom-up */
+  double level_ms[32];
+  double level_frontier[32];
+  double level_edges[32];
+  int32_t level_bu[32];
 } gbbfs_ms_stats;
 
 /* BFS depths from k sources.  depth_out (host) receives k rows of n entries,
@@ -171,6 +177,10 @@ int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
  * its k x n rows (valid until the next batched call on the handle). */
 int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
                        const void** depth_dev, gbbfs_ms_stats* st);
+
+/* HBM (bytes) the batched search state of an n-vertex graph takes: the
+ * figure the query server admits graphs against. */
+int64_t gbbfs_msbfs_state_bytes(int64_t n, int depth_bytes);
 
 /* Choose or read the batched configuration. */
 int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg);

@@ -96,8 +96,7 @@ def test_admission_budget(native, pool):
     exp = expected(native, pool)
     n_of = [g.n for _, g in pool]
     biggest = max(g.n for _, g in pool)
-    W = (biggest + 31) // 32
-    budget = 4 * 8 * biggest + 5 * 4 * biggest + 8 * W + 2 * 64 * biggest + (16 << 20)
+    budget = native.msbfs_state_bytes(biggest, 1)
     with native.Server(mode=0, hbm_budget_bytes=budget) as srv:
         for _, g in pool:
             srv.add_graph(g)
