@@ -488,17 +488,6 @@ int gbbfs_graph_create(const int64_t* offsets, const int32_t* neigh, int64_t n, 
   }
   gbbfs_graph* g = new (std::nothrow) gbbfs_graph();
   if (!g) return GBBFS_ERR_NOMEM;
-  // Hub list of the batched search (degree > kMsHubDeg), with chunk prefix.
-  uint64_t chunks = 0;
-  for (int64_t v = 0; v < n; v++) {
-    const int64_t d = offsets[v + 1] - offsets[v];
-    if (d > kMsHubDeg) {
-      g->hubs.push_back((int32_t)v);
-      g->hub_chunk.push_back((uint32_t)chunks);
-      chunks += (uint64_t)((d + kMsHubChunk - 1) / kMsHubChunk);
-    }
-  }
-  g->hub_chunk.push_back((uint32_t)chunks);
   int rc = create(offsets, neigh, n, m_dir, g);
   if (rc != GBBFS_OK) {
     release(g);

@@ -31,7 +31,7 @@ namespace gbbfs {
 // Asynchronous batch primitives of the multi-source search (msbfs.cu), used
 // by the query server.  Two depth buffers per handle; batches on one handle
 // run in stream order, batches on different handles overlap on the device.
-size_t ms_state_bytes(int64_t n, int64_t W, int depth_bytes);  // HBM a handle's state takes
+size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes);  // HBM a handle's state takes
 int ms_prepare(gbbfs_graph* g, int depth_bytes);   // allocate (or keep) the state
 int ms_lanes(const gbbfs_graph* g);
 int ms_launch(gbbfs_graph* g, int buf, const int32_t* sources, int k);
@@ -88,8 +88,4 @@ struct gbbfs_graph {
   bool have_result = false;
   bool result_depth = false;
   gbbfs::MsState* ms = nullptr;
-  // Vertices whose adjacency the batched search cuts into work chunks, and
-  // the exclusive prefix of their chunk counts (filled at graph creation).
-  std::vector<int32_t> hubs;
-  std::vector<uint32_t> hub_chunk;
 };

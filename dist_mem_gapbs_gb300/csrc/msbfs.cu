@@ -6,11 +6,17 @@
 // a plain DOBFS from source s gives vertex v, bit for bit.
 //
 // The kernel and the layout of its buffers are described in
-// msbfs_kernels.cuh.  This file owns the buffers, captures one CUDA graph per
-// batch buffer (sources copy, buffer resets, the persistent cooperative
-// kernel, a copy of the control block back to the host), runs batches back
-// to back with the copy of one batch's depths overlapping the next batch, and
-// holds the autotuner.  Depth rows are uint8 (255 = unreached) or int32 (-1).
+// msbfs_kernels.cuh.  The search runs on a copy of the graph in which the
+// vertices are grouped by the bit length of their degree, longest first
+// (isolated vertices last): the frontier words the bottom-up levels read at
+// random then gather on a compact, cache-resident range, and tiles hold
+// vertices of similar degree.  This file builds that copy when the state is
+// first made, owns the buffers, captures one CUDA graph per batch buffer
+// (sources copy, buffer resets, the persistent cooperative kernel, the two
+// passes that put the depth rows back into original vertex order, a copy of
+// the control block back to the host), runs batches back to back with the
+// copy of one batch's depths overlapping the next batch, and holds the
+// autotuner.  Depth rows are uint8 (255 = unreached) or int32 (-1).
 
 #include <cuda_runtime.h>
 
@@ -43,6 +49,12 @@ struct MsState {
   int32_t* hubs = nullptr;
   uint32_t* hub_chunk = nullptr;
   int64_t nhubs = 0;
+  void* roff = nullptr;              // search-ordered CSR (OffT offsets)
+  int32_t* rnbr = nullptr;
+  int32_t* perm = nullptr;           // original id -> search order id
+  void* dtmp = nullptr;              // depth rows in search order (row stride dstride)
+  int64_t dstride = 0;
+  void* drec = nullptr;              // per-vertex depth records, search order
   void* depth[2] = {nullptr, nullptr};
   int32_t* d_src[2] = {nullptr, nullptr};
   int32_t* h_src = nullptr;          // pinned, 2 x 64
@@ -83,6 +95,11 @@ void msbfs_release(MsState* ms) {
   cudaFree(ms->tq);
   cudaFree(ms->hubs);
   cudaFree(ms->hub_chunk);
+  cudaFree(ms->roff);
+  cudaFree(ms->rnbr);
+  cudaFree(ms->perm);
+  cudaFree(ms->dtmp);
+  cudaFree(ms->drec);
   if (ms->h_src) cudaFreeHost(ms->h_src);
   if (ms->h_ctl) cudaFreeHost(ms->h_ctl);
   if (ms->ev0) cudaEventDestroy(ms->ev0);
@@ -96,11 +113,14 @@ void msbfs_release(MsState* ms) {
 
 // Lane words are allocated at 64 bits so both lane widths fit: visit, the
 // two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
-// and tq; two frontier unions; two depth buffers of 64 rows; slack for the
-// hub list and control blocks.
-size_t ms_state_bytes(int64_t n, int64_t W, int depth_bytes) {
+// and tq; two frontier unions; the search-ordered CSR (offsets counted at 8
+// bytes) and its permutation; depth rows of 64 sources in search order, the
+// same as per-vertex records, two buffers of rows in original order; slack
+// for the hub list and control blocks.
+size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes) {
   return 4 * 8 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 8 * (size_t)W +
-         2 * (size_t)64 * n * depth_bytes + (16 << 20);
+         8 * (size_t)(n + 1) + 4 * (size_t)m + 4 * (size_t)n +
+         4 * (size_t)64 * (n + 128) * depth_bytes + (16 << 20);
 }
 
 namespace {
@@ -138,6 +158,89 @@ const void* kernel_for(const gbbfs_graph* g, const MsConfig& cfg, int depth_byte
                   : pick_kernel<unsigned long long>(cfg, depth_bytes);
 }
 
+// The search-ordered copy of the graph.  New ids: the vertices of degree
+// kMsOrderDeg or more in buckets by the bit length of their degree, longest
+// first, in id order inside each bucket; then the others in id order (a
+// counting sort on the host over the offsets).  Inside a bucket vertices keep
+// their order, so the rows put back into original order read from a few
+// sequential runs.  The neighbour lists are then copied and renamed on the
+// device.  Hubs (degree above kMsHubDeg) are listed in new-id order with
+// their work chunks' prefix.
+template <typename OffT, typename Alloc>
+int build_order(gbbfs_graph* g, MsState* ms, Alloc&& alloc) {
+  const int64_t n = g->n;
+  std::vector<OffT> hoff((size_t)n + 1);
+  GB_CUDA(cudaMemcpy(hoff.data(), g->off, sizeof(OffT) * (size_t)(n + 1),
+                     cudaMemcpyDeviceToHost));
+  auto deg = [&](int64_t v) { return (uint64_t)(hoff[v + 1] - hoff[v]); };
+  auto key = [&](int64_t v) {
+    const uint64_t d = deg(v);
+    if (d < (uint64_t)kMsOrderDeg) return 64;
+    int bits = 0;
+    for (uint64_t x = d; x; x >>= 1) bits++;
+    return 64 - bits;
+  };
+  std::vector<int64_t> pos(65, 0);
+  for (int64_t v = 0; v < n; v++) pos[key(v)]++;
+  int64_t run = 0;
+  for (auto& p : pos) {
+    const int64_t c = p;
+    p = run;
+    run += c;
+  }
+  std::vector<int32_t> perm((size_t)n), inv((size_t)n);
+  for (int64_t v = 0; v < n; v++) {
+    const int64_t r = pos[key(v)]++;
+    perm[v] = (int32_t)r;
+    inv[r] = (int32_t)v;
+  }
+  std::vector<OffT> noff((size_t)n + 1);
+  noff[0] = 0;
+  for (int64_t r = 0; r < n; r++) noff[r + 1] = noff[r] + (OffT)deg(inv[r]);
+  std::vector<int32_t> hubs;
+  std::vector<uint32_t> hub_chunk;
+  uint64_t chunks = 0;
+  for (int64_t r = 0; r < n; r++) {
+    if (deg(inv[r]) <= (uint64_t)kMsHubDeg) continue;
+    hubs.push_back((int32_t)r);
+    hub_chunk.push_back((uint32_t)chunks);
+    chunks += (deg(inv[r]) + kMsHubChunk - 1) / kMsHubChunk;
+  }
+  hub_chunk.push_back((uint32_t)chunks);
+
+  GB_TRY(alloc(&ms->roff, sizeof(OffT) * (size_t)(n + 1)));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->rnbr), 4 * (size_t)g->m));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->perm), 4 * (size_t)n));
+  int32_t* d_inv = nullptr;
+  GB_CUDA(cudaMalloc(&d_inv, 4 * (size_t)n));
+  cudaError_t e = cudaMemcpy(ms->roff, noff.data(), sizeof(OffT) * (size_t)(n + 1),
+                             cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(ms->perm, perm.data(), 4 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_inv, inv.data(), 4 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && g->m > 0) {
+    k_relabel_nbr<OffT><<<4 * g->sms, kThreads, 0, g->stream>>>(
+        reinterpret_cast<const OffT*>(g->off), g->nbr, reinterpret_cast<const OffT*>(ms->roff),
+        d_inv, ms->perm, ms->rnbr, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  cudaFree(d_inv);
+  if (e != cudaSuccess) {
+    ms_error = std::string("search-ordered graph copy: ") + cudaGetErrorString(e);
+    return GBBFS_ERR_CUDA;
+  }
+  ms->nhubs = (int64_t)hubs.size();
+  if (ms->nhubs) {
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->hubs), 4 * (size_t)ms->nhubs));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->hub_chunk), 4 * (size_t)(ms->nhubs + 1)));
+    GB_CUDA(cudaMemcpy(ms->hubs, hubs.data(), 4 * (size_t)ms->nhubs, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(ms->hub_chunk, hub_chunk.data(), 4 * (size_t)(ms->nhubs + 1),
+                       cudaMemcpyHostToDevice));
+  }
+  return GBBFS_OK;
+}
+
 int ensure_state(gbbfs_graph* g, int depth_bytes) {
   MsState* ms = g->ms;
   if (ms && ms->depth_bytes == depth_bytes) return GBBFS_OK;
@@ -148,7 +251,7 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
     g->ms = nullptr;
   }
   const int64_t n = g->n;
-  const size_t need = ms_state_bytes(n, g->W, depth_bytes);
+  const size_t need = ms_state_bytes(n, g->m, g->W, depth_bytes);
   size_t free_b = 0, total_b = 0;
   GB_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (need > free_b) {
@@ -177,16 +280,11 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[0]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[1]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
-  // Hubs (degree above kMsHubDeg) and the prefix of their work chunks.
-  ms->nhubs = (int64_t)g->hubs.size();
-  if (ms->nhubs) {
-    GB_TRY(alloc(reinterpret_cast<void**>(&ms->hubs), 4 * (size_t)ms->nhubs));
-    GB_TRY(alloc(reinterpret_cast<void**>(&ms->hub_chunk), 4 * (size_t)(ms->nhubs + 1)));
-    GB_CUDA(cudaMemcpy(ms->hubs, g->hubs.data(), 4 * (size_t)ms->nhubs,
-                       cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemcpy(ms->hub_chunk, g->hub_chunk.data(), 4 * (size_t)(ms->nhubs + 1),
-                       cudaMemcpyHostToDevice));
-  }
+  ms->dstride = (n + kDepthTile - 1) / kDepthTile * kDepthTile;
+  GB_TRY(alloc(&ms->dtmp, (size_t)kMsMaxLanes * ms->dstride * depth_bytes));
+  GB_TRY(alloc(&ms->drec, (size_t)kMsMaxLanes * n * depth_bytes));
+  GB_TRY(g->off32 ? build_order<uint32_t>(g, ms, alloc)
+                  : build_order<unsigned long long>(g, ms, alloc));
   for (int i = 0; i < 2; i++) {
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->q[i]), 4 * (size_t)n));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->qe[i]), 8 * (size_t)n));
@@ -222,8 +320,8 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   }
   ms->grid = per_sm * g->sms;
   MsArgs<OffT, LaneT, DepthT> a;
-  a.off = reinterpret_cast<const OffT*>(g->off);
-  a.nbr = g->nbr;
+  a.off = reinterpret_cast<const OffT*>(ms->roff);
+  a.nbr = ms->rnbr;
   a.n = g->n;
   a.m = g->m;
   a.visit = reinterpret_cast<LaneT*>(ms->visit);
@@ -241,8 +339,10 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.hubs = ms->hubs;
   a.hub_chunk = ms->hub_chunk;
   a.nhubs = ms->nhubs;
-  a.depth = reinterpret_cast<DepthT*>(ms->depth[buf]);
+  a.depth = reinterpret_cast<DepthT*>(ms->dtmp);
+  a.dstride = ms->dstride;
   a.sources = ms->d_src[buf];
+  a.perm = ms->perm;
   a.ctl = ms->ctl[buf];
   a.k = k;
   a.shift = g->shift;
@@ -259,8 +359,6 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->acc, 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->fbits[1], 0, 4 * (size_t)g->W, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->ctl[buf], 0, sizeof(MsCtl), s);
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(ms->depth[buf], 0xff, (size_t)k * g->n * sizeof(DepthT), s);
   if (e == cudaSuccess) {
     cudaLaunchConfig_t lc;
     memset(&lc, 0, sizeof lc);
@@ -275,6 +373,16 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
     lc.numAttrs = 1;
     void* args[] = {&a};
     e = cudaLaunchKernelExC(&lc, fn, args);
+  }
+  if (e == cudaSuccess) {
+    const unsigned blocks = (unsigned)((g->n + kDepthTile - 1) / kDepthTile);
+    k_depth_records<LaneT, DepthT><<<blocks, kThreads, 0, s>>>(
+        reinterpret_cast<const DepthT*>(ms->dtmp), ms->dstride,
+        reinterpret_cast<const LaneT*>(ms->visit), reinterpret_cast<DepthT*>(ms->drec), g->n, k);
+    k_depth_gather<DepthT><<<blocks, kThreads, 0, s>>>(
+        reinterpret_cast<const DepthT*>(ms->drec), ms->perm,
+        reinterpret_cast<DepthT*>(ms->depth[buf]), g->n, k);
+    e = cudaGetLastError();
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(ms->h_ctl + buf, ms->ctl[buf], sizeof(MsCtl), cudaMemcpyDeviceToHost, s);
@@ -525,9 +633,9 @@ int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg) {
   return GBBFS_OK;
 }
 
-int64_t gbbfs_msbfs_state_bytes(int64_t n, int depth_bytes) {
-  if (n < 0 || (depth_bytes != 1 && depth_bytes != 4)) return -1;
-  return (int64_t)gbbfs::ms_state_bytes(n, (n + 31) / 32, depth_bytes);
+int64_t gbbfs_msbfs_state_bytes(int64_t n, int64_t m_dir, int depth_bytes) {
+  if (n < 0 || m_dir < 0 || (depth_bytes != 1 && depth_bytes != 4)) return -1;
+  return (int64_t)gbbfs::ms_state_bytes(n, m_dir, (n + 31) / 32, depth_bytes);
 }
 
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,

@@ -51,6 +51,15 @@ enum MsPhase {
   kMsPhases
 };
 constexpr int kMsSmall = 32;        // bottom-up: lower degrees share a streamed pass
+// Vertices of at least this degree are numbered first in the search, in
+// buckets by the bit length of the degree, longest first; the others keep
+// their relative order after them (with 1: isolated vertices last).
+#ifndef GBBFS_MS_ORDER_DEG
+#define GBBFS_MS_ORDER_DEG 1
+#endif
+constexpr int kMsOrderDeg = GBBFS_MS_ORDER_DEG;
+constexpr int kDepthTile = 128;     // vertices per block of the depth record passes
+constexpr int kMsMaxLanes = 64;     // sources per batch at most (depth record length)
 constexpr int kMsGrab = 8;          // tiles of 32 vertices a warp takes at a time
 constexpr int kMsHubDeg = 2048;
 constexpr int kMsHubChunk = 2048;
@@ -93,8 +102,10 @@ struct MsArgs {
   const int32_t* hubs;
   const uint32_t* hub_chunk;   // nhubs + 1 entries
   int64_t nhubs;
-  DepthT* depth;
-  const int32_t* sources;
+  DepthT* depth;             // [source][search-order vertex] rows, only reached entries written
+  int64_t dstride;           // row stride of depth (elements, a multiple of kDepthTile)
+  const int32_t* sources;   // original vertex ids
+  const int32_t* perm;      // original id -> search order id
   MsCtl* ctl;
   int k;
   int shift;
@@ -343,10 +354,10 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
   // that is the source of several lanes is queued once.
   if (blockIdx.x == 0 && threadIdx.x < a.k) {
     const int i = threadIdx.x;
-    const int32_t s = a.sources[i];
+    const int32_t s = a.perm[a.sources[i]];
     const LaneT bit = (LaneT)1 << i;
     atomic_or_lane(a.visit + s, bit);
-    a.depth[(int64_t)i * a.n + s] = 0;
+    a.depth[(int64_t)i * a.dstride + s] = 0;
     if (atomic_or_lane(a.fr1 + s, bit) == 0) {
       const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
       if (deg) {
@@ -530,7 +541,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           }
           const unsigned nm = __ballot_sync(kFull, nb != 0);
           if (lane == 0) fbn[v0 >> 5] = nm;
-          write_depths(a.depth, a.n, v, nb, level);
+          write_depths(a.depth, a.dstride, v, nb, level);
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
@@ -564,7 +575,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
             if (nb) {
               a.visit[v] = vis | nb;
               for (LaneT x = nb; x; x &= x - 1)
-                a.depth[(int64_t)lowest_bit(x) * a.n + v] = (DepthT)level;
+                a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
               frn[v] = nb;
               atomicOr(fbn + (v >> 5), 1u << (v & 31));
               deg = (unsigned long long)(a.off[v + 1] - a.off[v]);
@@ -698,7 +709,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
         if (v < a.n) frn[v] = nb;
         const unsigned nm = __ballot_sync(kFull, nb != 0);
         if (lane == 0 && (v0 >> 5) < a.W) fbn[v0 >> 5] = nm;
-        write_depths(a.depth, a.n, v, nb, level);
+        write_depths(a.depth, a.dstride, v, nb, level);
         if (nb) {
           my_count++;
           my_edges += deg;
@@ -735,7 +746,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           if (nb) {
             a.visit[v] = vis | nb;
             for (LaneT x = nb; x; x &= x - 1)
-              a.depth[(int64_t)lowest_bit(x) * a.n + v] = (DepthT)level;
+              a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
             frn[v] = nb;
             atomicOr(fbn + (v >> 5), 1u << (v & 31));
             atomicAdd(nf_count, 1ull);
@@ -760,6 +771,162 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
   if (tid == 0) c->t_end = globaltimer();
   __syncthreads();
   if (threadIdx.x < kMsPhases) atomicAdd(&c->phase_cycles[threadIdx.x], ph_acc[threadIdx.x]);
+}
+
+// The search-ordered copy of the CSR: new vertex r is original vertex
+// inv[r], and every neighbour id is mapped through perm.  A warp per vertex.
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_relabel_nbr(const OffT* off, const int32_t* nbr,
+                                                          const OffT* noff, const int32_t* inv,
+                                                          const int32_t* perm, int32_t* nnbr,
+                                                          int64_t n) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    const int32_t u = inv[r];
+    const uint64_t b = (uint64_t)off[u];
+    const uint64_t d = (uint64_t)off[u + 1] - b;
+    const uint64_t nb = (uint64_t)noff[r];
+    for (uint64_t j = lane; j < d; j += 32) nnbr[nb + j] = perm[nbr[b + j]];
+  }
+}
+
+// Transpose of a 4x4 byte block: word j of the result holds byte j of each of
+// w[0..3] (w[0]'s in the low byte).
+__device__ __forceinline__ void transpose4x4(const uint32_t w[4], uint32_t r[4]) {
+  const uint32_t lo01 = __byte_perm(w[0], w[1], 0x5140), hi01 = __byte_perm(w[0], w[1], 0x7362);
+  const uint32_t lo23 = __byte_perm(w[2], w[3], 0x5140), hi23 = __byte_perm(w[2], w[3], 0x7362);
+  r[0] = __byte_perm(lo01, lo23, 0x5410);
+  r[1] = __byte_perm(lo01, lo23, 0x7632);
+  r[2] = __byte_perm(hi01, hi23, 0x5410);
+  r[3] = __byte_perm(hi01, hi23, 0x7632);
+}
+
+// Depth rows back to original vertex order, in two streaming passes.
+// k_depth_records: the search writes row i of source i in search order and
+// only at reached entries; a block turns kDepthTile vertices x all rows into
+// one record of kMsMaxLanes depths per vertex (vertex-major), filling the
+// entries whose visit bit is clear with the unreached value, so the rows need
+// no reset before a batch.  k_depth_gather: a block fetches the records of
+// kDepthTile consecutive original vertices through perm (whole records, so
+// the random reads use every byte they move) and writes each row's segment
+// coalesced.  Both go through shared memory with padded rows; uint8 depths
+// move as 4x4 byte blocks.
+template <typename LaneT, typename DepthT>
+__global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, int64_t stride,
+                                                            const LaneT* visit, DepthT* rec,
+                                                            int64_t n, int k) {
+  constexpr int kE = 16 / sizeof(DepthT);              // elements per 16-byte chunk
+  constexpr int kRowWords = kDepthTile * sizeof(DepthT) / 4 + 1;
+  __shared__ uint32_t tile[kMsMaxLanes * kRowWords];   // [row][vertex], padded rows
+  const int64_t p0 = (int64_t)blockIdx.x * kDepthTile;
+  constexpr int kChunks = kDepthTile / kE;             // chunks per row segment
+  for (int c = threadIdx.x; c < k * kChunks; c += blockDim.x) {
+    const int i = c / kChunks, j = c % kChunks;
+    const uint4 x = *reinterpret_cast<const uint4*>(rows + (int64_t)i * stride + p0 + j * kE);
+    uint32_t* t = tile + i * kRowWords + j * 4;
+    t[0] = x.x;
+    t[1] = x.y;
+    t[2] = x.z;
+    t[3] = x.w;
+  }
+  __syncthreads();
+  if constexpr (sizeof(DepthT) == 1) {
+    // 4 rows x 4 vertices per step: a word of each row, transposed into a
+    // word of each vertex's record; entries not reached become 0xff.
+    constexpr int kGroups = kMsMaxLanes / 4;
+    for (int t = threadIdx.x; t < kGroups * (kDepthTile / 4); t += blockDim.x) {
+      const int a4 = t % kGroups, b4 = t / kGroups;
+      uint32_t w[4], r[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int i = 4 * a4 + j;
+        w[j] = i < k ? tile[i * kRowWords + b4] : 0xffffffffu;
+      }
+      transpose4x4(w, r);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int64_t p = p0 + 4 * b4 + j;
+        if (p >= n) break;
+        uint32_t bits = 0;
+        if (4 * a4 < (int)(8 * sizeof(LaneT)))
+          bits = (uint32_t)((unsigned long long)visit[p] >> (4 * a4)) & 0xfu;
+        if (4 * a4 + 4 > k) bits &= (k > 4 * a4) ? ((1u << (k - 4 * a4)) - 1) : 0u;
+        const uint32_t m = ((bits * 0x204081u) & 0x01010101u) * 0xffu;
+        reinterpret_cast<uint32_t*>(rec + p * kMsMaxLanes)[a4] = (r[j] & m) | ~m;
+      }
+    }
+  } else {
+    constexpr int kRecChunks = kMsMaxLanes / kE;       // chunks per record
+    const DepthT* tb = reinterpret_cast<const DepthT*>(tile);
+    for (int t = threadIdx.x; t < kDepthTile * kRecChunks; t += blockDim.x) {
+      const int q = t / kRecChunks, c = t % kRecChunks;
+      const int64_t p = p0 + q;
+      if (p >= n) continue;
+      const LaneT vis = visit[p];
+      uint32_t w[4];
+      DepthT* e = reinterpret_cast<DepthT*>(w);
+#pragma unroll
+      for (int r = 0; r < kE; r++) {
+        const int i = c * kE + r;
+        const bool hit = i < k && i < (int)(8 * sizeof(LaneT)) && ((vis >> i) & 1);
+        e[r] = hit ? tb[(int64_t)i * kRowWords * (4 / sizeof(DepthT)) + q] : (DepthT)-1;
+      }
+      *reinterpret_cast<uint4*>(rec + p * kMsMaxLanes + c * kE) =
+          make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
+template <typename DepthT>
+__global__ void __launch_bounds__(kThreads) k_depth_gather(const DepthT* rec, const int32_t* perm,
+                                                           DepthT* out, int64_t n, int k) {
+  constexpr int kE = 16 / sizeof(DepthT);
+  constexpr int kRecWords = kMsMaxLanes * sizeof(DepthT) / 4 + 1;
+  __shared__ uint32_t tile[kDepthTile * kRecWords];    // [vertex][row], padded records
+  const int64_t v0 = (int64_t)blockIdx.x * kDepthTile;
+  constexpr int kRecChunks = kMsMaxLanes / kE;
+  const int used = (k + kE - 1) / kE;                  // chunks holding rows < k
+  for (int t = threadIdx.x; t < kDepthTile * kRecChunks; t += blockDim.x) {
+    const int q = t / kRecChunks, c = t % kRecChunks;
+    const int64_t v = v0 + q;
+    if (v >= n || c >= used) continue;
+    const int64_t p = perm[v];
+    const uint4 x = *reinterpret_cast<const uint4*>(rec + p * kMsMaxLanes + c * kE);
+    uint32_t* d = tile + q * kRecWords + c * 4;
+    d[0] = x.x;
+    d[1] = x.y;
+    d[2] = x.z;
+    d[3] = x.w;
+  }
+  __syncthreads();
+  if constexpr (sizeof(DepthT) == 1) {
+    if ((n & 3) == 0 && v0 + kDepthTile <= n) {
+      // 4 records x 4 rows per step: a word of each record, transposed into
+      // a word (4 consecutive vertices) of each row.
+      const int groups = (k + 3) / 4;
+      for (int t = threadIdx.x; t < groups * (kDepthTile / 4); t += blockDim.x) {
+        const int b4 = t % (kDepthTile / 4), a4 = t / (kDepthTile / 4);
+        uint32_t w[4], r[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) w[j] = tile[(4 * b4 + j) * kRecWords + a4];
+        transpose4x4(w, r);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int i = 4 * a4 + j;
+          if (i < k) *reinterpret_cast<uint32_t*>(out + (int64_t)i * n + v0 + 4 * b4) = r[j];
+        }
+      }
+      return;
+    }
+  }
+  const DepthT* tb = reinterpret_cast<const DepthT*>(tile);
+  for (int t = threadIdx.x; t < k * kDepthTile; t += blockDim.x) {
+    const int i = t / kDepthTile, q = t % kDepthTile;
+    const int64_t v = v0 + q;
+    if (v < n) out[(int64_t)i * n + v] = tb[(int64_t)q * kRecWords * (4 / sizeof(DepthT)) + i];
+  }
 }
 
 }  // namespace gbbfs

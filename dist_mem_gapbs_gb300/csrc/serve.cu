@@ -136,7 +136,7 @@ namespace {
 int64_t state_bytes_in_use(gbbfs_server* s) {
   int64_t b = 0;
   for (const Slot& sl : s->slots)
-    if (sl.admitted) b += (int64_t)ms_state_bytes(sl.g->n, sl.g->W, 1);
+    if (sl.admitted) b += (int64_t)ms_state_bytes(sl.g->n, sl.g->m, sl.g->W, 1);
   return b;
 }
 
@@ -144,7 +144,7 @@ int64_t state_bytes_in_use(gbbfs_server* s) {
 bool admit(gbbfs_server* s, size_t idx) {
   Slot& sl = s->slots[idx];
   if (sl.admitted) return true;
-  const int64_t need = (int64_t)ms_state_bytes(sl.g->n, sl.g->W, 1);
+  const int64_t need = (int64_t)ms_state_bytes(sl.g->n, sl.g->m, sl.g->W, 1);
   for (int pass = 0; pass < 2; pass++) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;

@@ -132,7 +132,7 @@ def lib():
             "gbbfs_msbfs_set_config": (I, [P, P]),
             "gbbfs_msbfs_get_config": (I, [P, P]),
             "gbbfs_msbfs_autotune": (I, [P, P, i64, I, P]),
-            "gbbfs_msbfs_state_bytes": (i64, [i64, I]),
+            "gbbfs_msbfs_state_bytes": (i64, [i64, i64, I]),
             "gbbfs_server_open": (I, [P, PP]),
             "gbbfs_server_add_graph": (I, [P, P, P]),
             "gbbfs_server_submit": (I, [P, i32, i32, P, P]),
@@ -398,9 +398,10 @@ def msbfs_get_config(g):
     return c.as_dict()
 
 
-def msbfs_state_bytes(n, depth_bytes=1):
-    """HBM bytes the batched search state of an n-vertex graph takes."""
-    r = lib().gbbfs_msbfs_state_bytes(int(n), int(depth_bytes))
+def msbfs_state_bytes(n, m_dir, depth_bytes=1):
+    """HBM bytes the batched search state of a graph with n vertices and
+    m_dir directed edges takes."""
+    r = lib().gbbfs_msbfs_state_bytes(int(n), int(m_dir), int(depth_bytes))
     if r < 0:
         raise ValueError("bad arguments to msbfs_state_bytes")
     return r

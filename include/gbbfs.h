@@ -178,9 +178,9 @@ int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
 int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
                        const void** depth_dev, gbbfs_ms_stats* st);
 
-/* HBM (bytes) the batched search state of an n-vertex graph takes: the
- * figure the query server admits graphs against. */
-int64_t gbbfs_msbfs_state_bytes(int64_t n, int depth_bytes);
+/* HBM (bytes) the batched search state of a graph with n vertices and m_dir
+ * directed edges takes: the figure the query server admits graphs against. */
+int64_t gbbfs_msbfs_state_bytes(int64_t n, int64_t m_dir, int depth_bytes);
 
 /* Choose or read the batched configuration. */
 int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg);

@@ -95,8 +95,7 @@ def test_admission_budget(native, pool):
     turns, every answer still exact."""
     exp = expected(native, pool)
     n_of = [g.n for _, g in pool]
-    biggest = max(g.n for _, g in pool)
-    budget = native.msbfs_state_bytes(biggest, 1)
+    budget = max(native.msbfs_state_bytes(g.n, g.m, 1) for _, g in pool)
     with native.Server(mode=0, hbm_budget_bytes=budget) as srv:
         for _, g in pool:
             srv.add_graph(g)
