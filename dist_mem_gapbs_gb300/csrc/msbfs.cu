@@ -1,4 +1,4 @@
-// Batched multi-source BFS: up to 64 sources per batch as a bitmask per vertex.
+// Batched multi-source BFS: up to 128 sources per batch as a bitmask per vertex.
 //
 // This form has no counterpart in the reference: it answers many BFS queries
 // of the same graph at once.  Its results are defined by the reference's
@@ -30,7 +30,7 @@
 namespace gbbfs {
 
 struct MsConfig {
-  int lanes = 64;        // 32 or 64 sources per batch
+  int lanes = 64;        // 32, 64 or 128 sources per batch
   int batch = 8;         // neighbours per bottom-up round of one thread
   int alpha = 15;        // top-down while frontier degrees <= m / alpha
 };
@@ -57,7 +57,7 @@ struct MsState {
   void* drec = nullptr;              // per-vertex depth records, search order
   void* depth[2] = {nullptr, nullptr};
   int32_t* d_src[2] = {nullptr, nullptr};
-  int32_t* h_src = nullptr;          // pinned, 2 x 64
+  int32_t* h_src = nullptr;          // pinned, 2 x kMsMaxLanes
   MsCtl* ctl[2] = {nullptr, nullptr};
   MsCtl* h_ctl = nullptr;            // pinned, 2
   cudaStream_t copy_stream = nullptr;
@@ -111,16 +111,16 @@ void msbfs_release(MsState* ms) {
 // ---------------------------------------------------------------------------
 // Host side.
 
-// Lane words are allocated at 64 bits so both lane widths fit: visit, the
+// Lane words are allocated at 128 bits so every lane width fits: visit, the
 // two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
 // and tq; two frontier unions; the search-ordered CSR (offsets counted at 8
-// bytes) and its permutation; depth rows of 64 sources in search order, the
+// bytes) and its permutation; depth rows of 128 sources in search order, the
 // same as per-vertex records, two buffers of rows in original order; slack
 // for the hub list and control blocks.
 size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes) {
-  return 4 * 8 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 8 * (size_t)W +
+  return 4 * 16 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 8 * (size_t)W +
          8 * (size_t)(n + 1) + 4 * (size_t)m + 4 * (size_t)n +
-         4 * (size_t)64 * (n + 128) * depth_bytes + (16 << 20);
+         4 * (size_t)kMsMaxLanes * (n + kDepthTile) * depth_bytes + (16 << 20);
 }
 
 namespace {
@@ -149,6 +149,7 @@ const void* pick_depth(int depth_bytes, int batch) {
 
 template <typename OffT>
 const void* pick_kernel(const MsConfig& cfg, int depth_bytes) {
+  if (cfg.lanes == 128) return pick_depth<OffT, Lane128>(depth_bytes, cfg.batch);
   return cfg.lanes == 32 ? pick_depth<OffT, uint32_t>(depth_bytes, cfg.batch)
                          : pick_depth<OffT, unsigned long long>(depth_bytes, cfg.batch);
 }
@@ -273,10 +274,10 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
     ms->bytes += (int64_t)bytes;
     return GBBFS_OK;
   };
-  GB_TRY(alloc(&ms->visit, 8 * (size_t)n));
-  GB_TRY(alloc(&ms->fr[0], 8 * (size_t)n));
-  GB_TRY(alloc(&ms->fr[1], 8 * (size_t)n));
-  GB_TRY(alloc(&ms->acc, 8 * (size_t)n));
+  GB_TRY(alloc(&ms->visit, sizeof(Lane128) * (size_t)n));
+  GB_TRY(alloc(&ms->fr[0], sizeof(Lane128) * (size_t)n));
+  GB_TRY(alloc(&ms->fr[1], sizeof(Lane128) * (size_t)n));
+  GB_TRY(alloc(&ms->acc, sizeof(Lane128) * (size_t)n));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[0]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[1]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
@@ -288,13 +289,13 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   for (int i = 0; i < 2; i++) {
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->q[i]), 4 * (size_t)n));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->qe[i]), 8 * (size_t)n));
-    GB_TRY(alloc(&ms->depth[i], (size_t)64 * n * depth_bytes));
-    GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), 64 * sizeof(int32_t)));
+    GB_TRY(alloc(&ms->depth[i], (size_t)kMsMaxLanes * n * depth_bytes));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), kMsMaxLanes * sizeof(int32_t)));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->ctl[i]), sizeof(MsCtl)));
     GB_CUDA(cudaEventCreateWithFlags(&ms->computed[i], cudaEventDisableTiming));
     GB_CUDA(cudaEventCreateWithFlags(&ms->copied[i], cudaEventDisableTiming));
   }
-  GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_src), 2 * 64 * sizeof(int32_t),
+  GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_src), 2 * kMsMaxLanes * sizeof(int32_t),
                         cudaHostAllocDefault));
   GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_ctl), 2 * sizeof(MsCtl),
                         cudaHostAllocDefault));
@@ -352,7 +353,8 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   cudaStream_t s = g->stream;
   const size_t lane_bytes = sizeof(LaneT) * (size_t)g->n;
   GB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = cudaMemcpyAsync(ms->d_src[buf], ms->h_src + 64 * buf, 64 * sizeof(int32_t),
+  cudaError_t e = cudaMemcpyAsync(ms->d_src[buf], ms->h_src + kMsMaxLanes * buf,
+                                  kMsMaxLanes * sizeof(int32_t),
                                   cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->visit, 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr[1], 0, lane_bytes, s);
@@ -375,7 +377,8 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
     e = cudaLaunchKernelExC(&lc, fn, args);
   }
   if (e == cudaSuccess) {
-    const unsigned blocks = (unsigned)((g->n + kDepthTile - 1) / kDepthTile);
+    constexpr int64_t kTileV = kDepthTile / (int64_t)sizeof(DepthT);
+    const unsigned blocks = (unsigned)((g->n + kTileV - 1) / kTileV);
     k_depth_records<LaneT, DepthT><<<blocks, kThreads, 0, s>>>(
         reinterpret_cast<const DepthT*>(ms->dtmp), ms->dstride,
         reinterpret_cast<const LaneT*>(ms->visit), reinterpret_cast<DepthT*>(ms->drec), g->n, k);
@@ -412,6 +415,7 @@ int capture_depth(gbbfs_graph* g, int buf, int k) {
 
 template <typename OffT>
 int capture_lanes(gbbfs_graph* g, int buf, int k) {
+  if (g->ms->cfg.lanes == 128) return capture_depth<OffT, Lane128>(g, buf, k);
   return g->ms->cfg.lanes == 32 ? capture_depth<OffT, uint32_t>(g, buf, k)
                                 : capture_depth<OffT, unsigned long long>(g, buf, k);
 }
@@ -440,7 +444,7 @@ int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
   // The host copy of the sources is read by the graph's first node; wait
   // until the previous launch that read this slot is done.
   GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
-  memcpy(ms->h_src + 64 * buf, sources, sizeof(int32_t) * k);
+  memcpy(ms->h_src + kMsMaxLanes * buf, sources, sizeof(int32_t) * k);
   GB_CUDA(cudaGraphLaunch(ms->exec[buf], g->stream));
   GB_CUDA(cudaEventRecord(ms->computed[buf], g->stream));
   return GBBFS_OK;
@@ -607,9 +611,9 @@ int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int de
 
 int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg) {
   if (!g || !cfg) return GBBFS_ERR_ARG;
-  if ((cfg->lanes != 32 && cfg->lanes != 64) ||
+  if ((cfg->lanes != 32 && cfg->lanes != 64 && cfg->lanes != 128) ||
       (cfg->batch != 4 && cfg->batch != 8 && cfg->batch != 16) || cfg->alpha < 1) {
-    last_error() = "lanes must be 32 or 64, batch 4, 8 or 16, alpha >= 1";
+    last_error() = "lanes must be 32, 64 or 128, batch 4, 8 or 16, alpha >= 1";
     return GBBFS_ERR_ARG;
   }
   GB_CUDA(cudaSetDevice(g->device));
@@ -641,7 +645,7 @@ int64_t gbbfs_msbfs_state_bytes(int64_t n, int64_t m_dir, int depth_bytes) {
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,
                          gbbfs_ms_config* best) {
   if (!g || !sample || k <= 0) return GBBFS_ERR_ARG;
-  static const int kLanes[] = {32, 64};
+  static const int kLanes[] = {32, 64, 128};
   static const int kBatches[] = {4, 8, 16};
   static const int kAlphas[] = {2, 6, 15, 40, 200};
   double best_t = 1e300;

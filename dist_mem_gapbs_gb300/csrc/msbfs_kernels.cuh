@@ -58,8 +58,8 @@ constexpr int kMsSmall = 32;        // bottom-up: lower degrees share a streamed
 #define GBBFS_MS_ORDER_DEG 1
 #endif
 constexpr int kMsOrderDeg = GBBFS_MS_ORDER_DEG;
-constexpr int kDepthTile = 128;     // vertices per block of the depth record passes
-constexpr int kMsMaxLanes = 64;     // sources per batch at most (depth record length)
+constexpr int kDepthTile = 128;     // bytes of each row per block of the depth record passes
+constexpr int kMsMaxLanes = 128;    // sources per batch at most (depth record length)
 constexpr int kMsGrab = 8;          // tiles of 32 vertices a warp takes at a time
 constexpr int kMsHubDeg = 2048;
 constexpr int kMsHubChunk = 2048;
@@ -113,35 +113,141 @@ struct MsArgs {
   unsigned long long limit_ns;
 };
 
+// A lane word of 128 sources (two 64-bit halves, lo = sources 0..63).
+struct __align__(16) Lane128 {
+  unsigned long long lo, hi;
+  Lane128() = default;
+  __host__ __device__ constexpr Lane128(unsigned long long x) : lo(x), hi(0) {}
+  __host__ __device__ constexpr Lane128(unsigned long long l, unsigned long long h) : lo(l), hi(h) {}
+  __host__ __device__ explicit operator bool() const { return (lo | hi) != 0; }
+};
+__host__ __device__ inline Lane128 operator&(Lane128 a, Lane128 b) { return {a.lo & b.lo, a.hi & b.hi}; }
+__host__ __device__ inline Lane128 operator|(Lane128 a, Lane128 b) { return {a.lo | b.lo, a.hi | b.hi}; }
+__host__ __device__ inline Lane128 operator~(Lane128 a) { return {~a.lo, ~a.hi}; }
+__host__ __device__ inline Lane128& operator&=(Lane128& a, Lane128 b) { return a = a & b; }
+__host__ __device__ inline Lane128& operator|=(Lane128& a, Lane128 b) { return a = a | b; }
+__host__ __device__ inline bool operator==(Lane128 a, Lane128 b) { return a.lo == b.lo && a.hi == b.hi; }
+__host__ __device__ inline bool operator!=(Lane128 a, Lane128 b) { return !(a == b); }
+
+__device__ __forceinline__ Lane128 shfl(Lane128 x, int src) {
+  return {shfl(x.lo, src), shfl(x.hi, src)};
+}
+
+// Lane-word helpers for the three widths (uint32, uint64, Lane128).
 template <typename LaneT>
-__device__ __forceinline__ LaneT atomic_or_lane(LaneT* p, LaneT v) {
-  if constexpr (sizeof(LaneT) == 8)
-    return (LaneT)atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+__device__ __forceinline__ uint32_t word32(LaneT x, int h) {   // 32-bit word h
+  if constexpr (sizeof(LaneT) == 16)
+    return (uint32_t)((h < 2 ? x.lo : x.hi) >> (32 * (h & 1)));
   else
-    return (LaneT)atomicOr(reinterpret_cast<unsigned int*>(p), (unsigned int)v);
+    return (uint32_t)((unsigned long long)x >> (32 * h));
 }
 
 template <typename LaneT>
-__device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
-  if constexpr (sizeof(LaneT) == 8)
-    return (LaneT)__ldcg(reinterpret_cast<const unsigned long long*>(p));
+__device__ __forceinline__ LaneT from_words(const uint32_t* w) {
+  if constexpr (sizeof(LaneT) == 16)
+    return Lane128(((unsigned long long)w[1] << 32) | w[0], ((unsigned long long)w[3] << 32) | w[2]);
+  else if constexpr (sizeof(LaneT) == 8)
+    return (LaneT)(((unsigned long long)w[1] << 32) | w[0]);
   else
-    return (LaneT)__ldcg(reinterpret_cast<const unsigned int*>(p));
+    return (LaneT)w[0];
 }
 
 template <typename LaneT>
-__device__ __forceinline__ LaneT warp_or(LaneT x) {
-#pragma unroll
-  for (int o = 16; o; o >>= 1) x |= shfl(x, (int)(threadIdx.x & 31) ^ o);
-  return x;
+__device__ __forceinline__ bool lane_test(LaneT x, int i) {
+  return (word32(x, i >> 5) >> (i & 31)) & 1u;
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT lane_bit(int i) {
+  if constexpr (sizeof(LaneT) == 16)
+    return i < 64 ? Lane128(1ull << i, 0) : Lane128(0, 1ull << (i - 64));
+  else
+    return (LaneT)((LaneT)1 << i);
+}
+
+// The k lowest lanes.
+template <typename LaneT>
+__device__ __forceinline__ LaneT lane_ones(int k) {
+  if constexpr (sizeof(LaneT) == 16)
+    return Lane128(k >= 64 ? ~0ull : (1ull << k) - 1,
+                   k >= 128 ? ~0ull : k > 64 ? (1ull << (k - 64)) - 1 : 0ull);
+  else
+    return k >= (int)(8 * sizeof(LaneT)) ? (LaneT)~(LaneT)0 : (LaneT)(((LaneT)1 << k) - 1);
 }
 
 template <typename LaneT>
 __device__ __forceinline__ int lowest_bit(LaneT x) {
-  if constexpr (sizeof(LaneT) == 8)
+  if constexpr (sizeof(LaneT) == 16)
+    return x.lo ? __ffsll((long long)x.lo) - 1 : 63 + __ffsll((long long)x.hi);
+  else if constexpr (sizeof(LaneT) == 8)
     return __ffsll((long long)x) - 1;
   else
     return __ffs((int)x) - 1;
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT clear_lowest(LaneT x) {
+  if constexpr (sizeof(LaneT) == 16)
+    return x.lo ? Lane128(x.lo & (x.lo - 1), x.hi) : Lane128(0, x.hi & (x.hi - 1));
+  else
+    return (LaneT)(x & (x - 1));
+}
+
+// OR into a lane word in global memory (result not needed).
+template <typename LaneT>
+__device__ __forceinline__ void atomic_or_lane(LaneT* p, LaneT v) {
+  if constexpr (sizeof(LaneT) == 16) {
+    if (v.lo) atomicOr(&p->lo, v.lo);
+    if (v.hi) atomicOr(&p->hi, v.hi);
+  } else if constexpr (sizeof(LaneT) == 8) {
+    atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+  } else {
+    atomicOr(reinterpret_cast<unsigned int*>(p), (unsigned int)v);
+  }
+}
+
+// OR into a lane word; true for the call that first made it non-zero.  A
+// 128-lane word is two 64-bit atomics, so there each half has its own first
+// caller: a word can report two first touches, never none.
+template <typename LaneT>
+__device__ __forceinline__ bool first_or_lane(LaneT* p, LaneT v) {
+  if constexpr (sizeof(LaneT) == 16) {
+    bool first = false;
+    if (v.lo) first |= atomicOr(&p->lo, v.lo) == 0;
+    if (v.hi) first |= atomicOr(&p->hi, v.hi) == 0;
+    return first;
+  } else if constexpr (sizeof(LaneT) == 8) {
+    return atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v) == 0;
+  } else {
+    return atomicOr(reinterpret_cast<unsigned int*>(p), (unsigned int)v) == 0;
+  }
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
+  if constexpr (sizeof(LaneT) == 16) {
+    const ulonglong2 t = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+    return Lane128(t.x, t.y);
+  } else if constexpr (sizeof(LaneT) == 8) {
+    return (LaneT)__ldcg(reinterpret_cast<const unsigned long long*>(p));
+  } else {
+    return (LaneT)__ldcg(reinterpret_cast<const unsigned int*>(p));
+  }
+}
+
+// OR over the lanes of `grp` (the calling lane included), one warp reduction
+// per 32-bit word.
+template <typename LaneT>
+__device__ __forceinline__ LaneT group_or(unsigned grp, LaneT x) {
+  uint32_t w[4];
+#pragma unroll
+  for (int h = 0; h < (int)(sizeof(LaneT) / 4); h++) w[h] = __reduce_or_sync(grp, word32(x, h));
+  return from_words<LaneT>(w);
+}
+
+template <typename LaneT>
+__device__ __forceinline__ LaneT warp_or(LaneT x) {
+  return group_or(kFull, x);
 }
 
 // Frontier words and bits are read with L1-cached loads: they are written
@@ -204,9 +310,9 @@ __device__ __forceinline__ void write_depths(DepthT* depth, int64_t n, int64_t v
   const DepthT d = (DepthT)level;
 #pragma unroll
   for (int h = 0; h < (int)(sizeof(LaneT) / 4); h++) {
-    unsigned anyh = (unsigned)((unsigned long long)any >> (32 * h));
+    unsigned anyh = word32(any, h);
     if (!anyh) continue;
-    unsigned bits = (unsigned)((unsigned long long)nb >> (32 * h));
+    unsigned bits = word32(nb, h);
     DepthT* p = depth + (int64_t)(32 * h) * n + v;
     if (__popc(anyh) > 12) {
 #pragma unroll 8
@@ -328,8 +434,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
   const int64_t warp = tid >> 5;
   const int64_t nwarps = nthreads >> 5;
   const unsigned long long emask = (1ull << a.shift) - 1;
-  const LaneT all = a.k >= (int)(8 * sizeof(LaneT)) ? (LaneT)~(LaneT)0
-                                                     : (LaneT)(((LaneT)1 << a.k) - 1);
+  const LaneT all = lane_ones<LaneT>(a.k);
   const int max_level = sizeof(DepthT) == 1 ? 254 : 0x7ffffffe;
   const int64_t hub_chunks = a.nhubs ? (int64_t)a.hub_chunk[a.nhubs] : 0;
   if (tid == 0) c->t_begin = globaltimer();
@@ -355,10 +460,10 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
   if (blockIdx.x == 0 && threadIdx.x < a.k) {
     const int i = threadIdx.x;
     const int32_t s = a.perm[a.sources[i]];
-    const LaneT bit = (LaneT)1 << i;
+    const LaneT bit = lane_bit<LaneT>(i);
     atomic_or_lane(a.visit + s, bit);
     a.depth[(int64_t)i * a.dstride + s] = 0;
-    if (atomic_or_lane(a.fr1 + s, bit) == 0) {
+    if (first_or_lane(a.fr1 + s, bit)) {
       const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
       if (deg) {
         const unsigned long long at = atomicAdd(&c->q_packed[1], (1ull << a.shift) + deg);
@@ -506,7 +611,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
               atomic_or_lane(a.acc + v, f_s);
             } else {
               const LaneT nb = f_s & ~ld_lane(a.visit + v);
-              if (nb) first = atomic_or_lane(a.acc + v, nb) == 0;
+              if (nb) first = first_or_lane(a.acc + v, nb);
             }
           }
           if (!dense) warp_append(touched, a.tq, first, v);
@@ -574,7 +679,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
             nb &= ~vis;
             if (nb) {
               a.visit[v] = vis | nb;
-              for (LaneT x = nb; x; x &= x - 1)
+              for (LaneT x = nb; x; x = clear_lowest(x))
                 a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
               frn[v] = nb;
               atomicOr(fbn + (v >> 5), 1u << (v & 31));
@@ -628,7 +733,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
             const LaneT got = warp_gather_or(a.nbr, fb, fr, b, e, vis, all, filter);
             const LaneT part = got & ~vis & all;
             bool first = false;
-            if (lane == 0 && part) first = atomic_or_lane(a.acc + v, part) == 0;
+            if (lane == 0 && part) first = first_or_lane(a.acc + v, part);
             warp_append(touched, a.tq, first, v);
           }
           mark(kPhHub);
@@ -680,14 +785,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           for (int r = 0; r < kR; r++) {
             const LaneT x = in[r] ? ld_frontier(fr + u[r]) : (LaneT)0;
             const unsigned grp = __match_any_sync(kFull, o[r]);
-            LaneT red;
-            if constexpr (sizeof(LaneT) == 8) {
-              const unsigned lo = __reduce_or_sync(grp, (unsigned)x);
-              const unsigned hi = __reduce_or_sync(grp, (unsigned)((unsigned long long)x >> 32));
-              red = (LaneT)(((unsigned long long)hi << 32) | lo);
-            } else {
-              red = (LaneT)__reduce_or_sync(grp, (unsigned)x);
-            }
+            const LaneT red = group_or(grp, x);
             if (o[r] < 32u && red && lane == __ffs(grp) - 1) tacc[o[r]] |= red;
           }
         }
@@ -745,7 +843,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           nb &= ~vis;
           if (nb) {
             a.visit[v] = vis | nb;
-            for (LaneT x = nb; x; x &= x - 1)
+            for (LaneT x = nb; x; x = clear_lowest(x))
               a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
             frn[v] = nb;
             atomicOr(fbn + (v >> 5), 1u << (v & 31));
@@ -805,11 +903,11 @@ __device__ __forceinline__ void transpose4x4(const uint32_t w[4], uint32_t r[4])
 
 // Depth rows back to original vertex order, in two streaming passes.
 // k_depth_records: the search writes row i of source i in search order and
-// only at reached entries; a block turns kDepthTile vertices x all rows into
+// only at reached entries; a block turns kDepthTile bytes of every row into
 // one record of kMsMaxLanes depths per vertex (vertex-major), filling the
 // entries whose visit bit is clear with the unreached value, so the rows need
 // no reset before a batch.  k_depth_gather: a block fetches the records of
-// kDepthTile consecutive original vertices through perm (whole records, so
+// consecutive original vertices through perm (whole records, so
 // the random reads use every byte they move) and writes each row's segment
 // coalesced.  Both go through shared memory with padded rows; uint8 depths
 // move as 4x4 byte blocks.
@@ -818,10 +916,11 @@ __global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, 
                                                             const LaneT* visit, DepthT* rec,
                                                             int64_t n, int k) {
   constexpr int kE = 16 / sizeof(DepthT);              // elements per 16-byte chunk
-  constexpr int kRowWords = kDepthTile * sizeof(DepthT) / 4 + 1;
+  constexpr int kTileV = kDepthTile / (int)sizeof(DepthT);   // vertices per block
+  constexpr int kRowWords = kTileV * sizeof(DepthT) / 4 + 1;
   __shared__ uint32_t tile[kMsMaxLanes * kRowWords];   // [row][vertex], padded rows
-  const int64_t p0 = (int64_t)blockIdx.x * kDepthTile;
-  constexpr int kChunks = kDepthTile / kE;             // chunks per row segment
+  const int64_t p0 = (int64_t)blockIdx.x * kTileV;
+  constexpr int kChunks = kTileV / kE;             // chunks per row segment
   for (int c = threadIdx.x; c < k * kChunks; c += blockDim.x) {
     const int i = c / kChunks, j = c % kChunks;
     const uint4 x = *reinterpret_cast<const uint4*>(rows + (int64_t)i * stride + p0 + j * kE);
@@ -836,7 +935,7 @@ __global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, 
     // 4 rows x 4 vertices per step: a word of each row, transposed into a
     // word of each vertex's record; entries not reached become 0xff.
     constexpr int kGroups = kMsMaxLanes / 4;
-    for (int t = threadIdx.x; t < kGroups * (kDepthTile / 4); t += blockDim.x) {
+    for (int t = threadIdx.x; t < kGroups * (kTileV / 4); t += blockDim.x) {
       const int a4 = t % kGroups, b4 = t / kGroups;
       uint32_t w[4], r[4];
 #pragma unroll
@@ -851,7 +950,7 @@ __global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, 
         if (p >= n) break;
         uint32_t bits = 0;
         if (4 * a4 < (int)(8 * sizeof(LaneT)))
-          bits = (uint32_t)((unsigned long long)visit[p] >> (4 * a4)) & 0xfu;
+          bits = (word32(visit[p], a4 >> 3) >> (4 * (a4 & 7))) & 0xfu;
         if (4 * a4 + 4 > k) bits &= (k > 4 * a4) ? ((1u << (k - 4 * a4)) - 1) : 0u;
         const uint32_t m = ((bits * 0x204081u) & 0x01010101u) * 0xffu;
         reinterpret_cast<uint32_t*>(rec + p * kMsMaxLanes)[a4] = (r[j] & m) | ~m;
@@ -860,7 +959,7 @@ __global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, 
   } else {
     constexpr int kRecChunks = kMsMaxLanes / kE;       // chunks per record
     const DepthT* tb = reinterpret_cast<const DepthT*>(tile);
-    for (int t = threadIdx.x; t < kDepthTile * kRecChunks; t += blockDim.x) {
+    for (int t = threadIdx.x; t < kTileV * kRecChunks; t += blockDim.x) {
       const int q = t / kRecChunks, c = t % kRecChunks;
       const int64_t p = p0 + q;
       if (p >= n) continue;
@@ -870,7 +969,7 @@ __global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, 
 #pragma unroll
       for (int r = 0; r < kE; r++) {
         const int i = c * kE + r;
-        const bool hit = i < k && i < (int)(8 * sizeof(LaneT)) && ((vis >> i) & 1);
+        const bool hit = i < k && i < (int)(8 * sizeof(LaneT)) && lane_test(vis, i);
         e[r] = hit ? tb[(int64_t)i * kRowWords * (4 / sizeof(DepthT)) + q] : (DepthT)-1;
       }
       *reinterpret_cast<uint4*>(rec + p * kMsMaxLanes + c * kE) =
@@ -883,12 +982,13 @@ template <typename DepthT>
 __global__ void __launch_bounds__(kThreads) k_depth_gather(const DepthT* rec, const int32_t* perm,
                                                            DepthT* out, int64_t n, int k) {
   constexpr int kE = 16 / sizeof(DepthT);
+  constexpr int kTileV = kDepthTile / (int)sizeof(DepthT);   // vertices per block
   constexpr int kRecWords = kMsMaxLanes * sizeof(DepthT) / 4 + 1;
-  __shared__ uint32_t tile[kDepthTile * kRecWords];    // [vertex][row], padded records
-  const int64_t v0 = (int64_t)blockIdx.x * kDepthTile;
+  __shared__ uint32_t tile[kTileV * kRecWords];    // [vertex][row], padded records
+  const int64_t v0 = (int64_t)blockIdx.x * kTileV;
   constexpr int kRecChunks = kMsMaxLanes / kE;
   const int used = (k + kE - 1) / kE;                  // chunks holding rows < k
-  for (int t = threadIdx.x; t < kDepthTile * kRecChunks; t += blockDim.x) {
+  for (int t = threadIdx.x; t < kTileV * kRecChunks; t += blockDim.x) {
     const int q = t / kRecChunks, c = t % kRecChunks;
     const int64_t v = v0 + q;
     if (v >= n || c >= used) continue;
@@ -902,12 +1002,12 @@ __global__ void __launch_bounds__(kThreads) k_depth_gather(const DepthT* rec, co
   }
   __syncthreads();
   if constexpr (sizeof(DepthT) == 1) {
-    if ((n & 3) == 0 && v0 + kDepthTile <= n) {
+    if ((n & 3) == 0 && v0 + kTileV <= n) {
       // 4 records x 4 rows per step: a word of each record, transposed into
       // a word (4 consecutive vertices) of each row.
       const int groups = (k + 3) / 4;
-      for (int t = threadIdx.x; t < groups * (kDepthTile / 4); t += blockDim.x) {
-        const int b4 = t % (kDepthTile / 4), a4 = t / (kDepthTile / 4);
+      for (int t = threadIdx.x; t < groups * (kTileV / 4); t += blockDim.x) {
+        const int b4 = t % (kTileV / 4), a4 = t / (kTileV / 4);
         uint32_t w[4], r[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) w[j] = tile[(4 * b4 + j) * kRecWords + a4];
@@ -922,8 +1022,8 @@ __global__ void __launch_bounds__(kThreads) k_depth_gather(const DepthT* rec, co
     }
   }
   const DepthT* tb = reinterpret_cast<const DepthT*>(tile);
-  for (int t = threadIdx.x; t < k * kDepthTile; t += blockDim.x) {
-    const int i = t / kDepthTile, q = t % kDepthTile;
+  for (int t = threadIdx.x; t < k * kTileV; t += blockDim.x) {
+    const int i = t / kTileV, q = t % kTileV;
     const int64_t v = v0 + q;
     if (v < n) out[(int64_t)i * n + v] = tb[(int64_t)q * kRecWords * (4 / sizeof(DepthT)) + i];
   }

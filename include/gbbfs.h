@@ -133,13 +133,13 @@ int gbbfs_result_device_ptrs(gbbfs_graph* g, const int32_t** parent,
                              const int32_t** depth);
 
 /* ---- Batched multi-source BFS (no reference counterpart) ----
- * Many sources of one graph at once, 32 or 64 per batch as a bitmask per
+ * Many sources of one graph at once, 32, 64 or 128 per batch as a bitmask per
  * vertex, in one persistent kernel per batch captured in a CUDA graph.  Its
  * results are defined by the single-source search above: depth[s][v] equals
  * the depth gbbfs_bfs (and the reference's DOBFS, src/bfs.cc:142-188) gives v
  * from sources[s]. */
 typedef struct gbbfs_ms_config {
-  int32_t lanes;  /* sources per batch: 32 or 64                         */
+  int32_t lanes;  /* sources per batch: 32, 64 or 128                    */
   int32_t batch;  /* neighbours one thread reads per bottom-up round: 4, 8, 16 */
   int32_t alpha;  /* a level runs top-down while its frontier's summed degree
                      is <= m_dir / alpha, bottom-up above                 */

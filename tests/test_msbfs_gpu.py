@@ -17,7 +17,8 @@ def as_int32(d):
 
 
 @pytest.mark.parametrize("lanes,batch,alpha", [(64, 8, 15), (32, 4, 2), (64, 16, 200),
-                                               (32, 8, 6), (64, 4, 1)])
+                                               (32, 8, 6), (64, 4, 1), (128, 8, 15),
+                                               (128, 4, 2), (128, 16, 200)])
 def test_msbfs_matches_single_source(native, lanes, batch, alpha):
     off, nbr = native.make_graph(16, 16, False)
     with native.Graph(off, nbr) as g:
@@ -32,11 +33,13 @@ def test_msbfs_matches_single_source(native, lanes, batch, alpha):
         assert np.array_equal(d32, ref)
 
 
-@pytest.mark.parametrize("scale,uniform", [(15, True), (18, False)])
-def test_msbfs_graphs(native, scale, uniform):
+@pytest.mark.parametrize("scale,uniform,lanes", [(15, True, 64), (18, False, 64),
+                                                 (15, True, 128), (18, False, 128)])
+def test_msbfs_graphs(native, scale, uniform, lanes):
     off, nbr = native.make_graph(scale, 16, uniform)
     with native.Graph(off, nbr) as g:
-        srcs = native.pick_sources(off, 64)
+        native.msbfs_set_config(g, lanes, 8, 15)
+        srcs = native.pick_sources(off, 200)
         ref = single_depths(native, g, srcs)
         assert np.array_equal(native.msbfs(g, srcs, 4), ref)
         # fewer sources than lanes, duplicate sources, any order
@@ -61,8 +64,9 @@ def test_msbfs_handmade(native):
         assert np.array_equal(as_int32(native.msbfs(g, ok, 1)), ref[[1, 3, 4]])
 
 
-@pytest.mark.parametrize("alpha", [1, 15, 100000])
-def test_msbfs_hubs(native, alpha):
+@pytest.mark.parametrize("alpha,lanes", [(1, 64), (15, 64), (100000, 64), (1, 128),
+                                         (100000, 128)])
+def test_msbfs_hubs(native, alpha, lanes):
     """Vertices above the hub degree are cut into work chunks in both directions."""
     rng = np.random.default_rng(3)
     edges = np.concatenate([
@@ -75,8 +79,9 @@ def test_msbfs_hubs(native, alpha):
         srcs = np.array([0, 9001, int(np.argmax(deg[1:]) + 1)] +
                         list(native.pick_sources(off, 40)), np.int32)
         ref = single_depths(native, g, srcs)
-        native.msbfs_set_config(g, 64, 8, alpha)
+        native.msbfs_set_config(g, lanes, 8, alpha)
         assert np.array_equal(native.msbfs(g, srcs, 4), ref)
+        assert np.array_equal(as_int32(native.msbfs(g, srcs, 1)), ref)
 
 
 def test_msbfs_device_and_autotune(native):
@@ -84,7 +89,7 @@ def test_msbfs_device_and_autotune(native):
     with native.Graph(off, nbr) as g:
         srcs = native.pick_sources(off, 64)
         best = native.msbfs_autotune(g, srcs, 1)
-        assert best["lanes"] in (32, 64) and best["batch"] in (4, 8, 16)
+        assert best["lanes"] in (32, 64, 128) and best["batch"] in (4, 8, 16)
         assert native.msbfs_get_config(g) == best
         ref = single_depths(native, g, srcs)
         assert np.array_equal(as_int32(native.msbfs(g, srcs, 1)), ref)
