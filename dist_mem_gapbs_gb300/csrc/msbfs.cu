@@ -49,6 +49,8 @@ struct MsState {
   int32_t* hubs = nullptr;
   uint32_t* hub_chunk = nullptr;
   int64_t nhubs = 0;
+  int32_t* unit_tile = nullptr;      // bottom-up work units (tile ranges)
+  int64_t nunits = 0;
   void* roff = nullptr;              // search-ordered CSR (OffT offsets)
   int32_t* rnbr = nullptr;
   int32_t* perm = nullptr;           // original id -> search order id
@@ -95,6 +97,7 @@ void msbfs_release(MsState* ms) {
   cudaFree(ms->tq);
   cudaFree(ms->hubs);
   cudaFree(ms->hub_chunk);
+  cudaFree(ms->unit_tile);
   cudaFree(ms->roff);
   cudaFree(ms->rnbr);
   cudaFree(ms->perm);
@@ -113,12 +116,12 @@ void msbfs_release(MsState* ms) {
 
 // Lane words are allocated at 128 bits so every lane width fits: visit, the
 // two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
-// and tq; two frontier unions; the search-ordered CSR (offsets counted at 8
+// and tq; two frontier unions and the work-unit table; the search-ordered CSR (offsets counted at 8
 // bytes) and its permutation; depth rows of 128 sources in search order, the
 // same as per-vertex records, two buffers of rows in original order; slack
 // for the hub list and control blocks.
 size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes) {
-  return 4 * 16 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 8 * (size_t)W +
+  return 4 * 16 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 12 * (size_t)(W + 1) +
          8 * (size_t)(n + 1) + 4 * (size_t)m + 4 * (size_t)n +
          4 * (size_t)kMsMaxLanes * (n + kDepthTile) * depth_bytes + (16 << 20);
 }
@@ -208,6 +211,31 @@ int build_order(gbbfs_graph* g, MsState* ms, Alloc&& alloc) {
     chunks += (deg(inv[r]) + kMsHubChunk - 1) / kMsHubChunk;
   }
   hub_chunk.push_back((uint32_t)chunks);
+  // Bottom-up work units: runs of up to kMsGrab tiles, cut early once the
+  // tiles' non-hub vertices hold kMsUnitEdges edges, so the high-degree
+  // tiles at the front of the order do not pile up on one warp.
+  std::vector<int32_t> unit_tile;
+  const int64_t tiles = (n + 31) / 32;
+  {
+    int64_t in_unit = 0;
+    uint64_t edges = 0;
+    for (int64_t t = 0; t < tiles; t++) {
+      if (in_unit == 0) unit_tile.push_back((int32_t)t);
+      for (int64_t r = 32 * t; r < std::min<int64_t>(n, 32 * t + 32); r++) {
+        const uint64_t d = deg(inv[r]);
+        if (d <= (uint64_t)kMsHubDeg) edges += d;
+      }
+      if (++in_unit == kMsGrab || edges >= (uint64_t)kMsUnitEdges) {
+        in_unit = 0;
+        edges = 0;
+      }
+    }
+    unit_tile.push_back((int32_t)tiles);
+  }
+  ms->nunits = (int64_t)unit_tile.size() - 1;
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->unit_tile), 4 * unit_tile.size()));
+  GB_CUDA(cudaMemcpy(ms->unit_tile, unit_tile.data(), 4 * unit_tile.size(),
+                     cudaMemcpyHostToDevice));
 
   GB_TRY(alloc(&ms->roff, sizeof(OffT) * (size_t)(n + 1)));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->rnbr), 4 * (size_t)g->m));
@@ -338,6 +366,8 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.qe1 = ms->qe[1];
   a.tq = ms->tq;
   a.hubs = ms->hubs;
+  a.unit_tile = ms->unit_tile;
+  a.nunits = ms->nunits;
   a.hub_chunk = ms->hub_chunk;
   a.nhubs = ms->nhubs;
   a.depth = reinterpret_cast<DepthT*>(ms->dtmp);

@@ -27,7 +27,8 @@
 //     word.  A frontier that was written densely is queued from its fbits
 //     when a top-down level needs it.
 //   bottom-up: a warp per tile of 32 consecutive vertices, tiles handed out
-//     kMsGrab at a time from a counter.  The concatenated adjacency of the
+//     in work units from a counter (up to kMsGrab tiles, fewer where the
+//     tiles hold many edges).  The concatenated adjacency of the
 //     tile's unfinished vertices of degree below kMsSmall is streamed 32
 //     edges per lane-step into per-vertex words in shared memory; vertices
 //     up to kMsHubDeg get the whole warp with early exit once every lane is
@@ -60,7 +61,8 @@ constexpr int kMsSmall = 32;        // bottom-up: lower degrees share a streamed
 constexpr int kMsOrderDeg = GBBFS_MS_ORDER_DEG;
 constexpr int kDepthTile = 128;     // bytes of each row per block of the depth record passes
 constexpr int kMsMaxLanes = 128;    // sources per batch at most (depth record length)
-constexpr int kMsGrab = 8;          // tiles of 32 vertices a warp takes at a time
+constexpr int kMsGrab = 8;          // tiles of 32 vertices in a bottom-up work unit at most
+constexpr int kMsUnitEdges = 4096;  // a unit also ends once its tiles hold this many edges
 constexpr int kMsHubDeg = 2048;
 constexpr int kMsHubChunk = 2048;
 constexpr int kMsTdSpan = 2048;     // edges per warp span of a top-down level
@@ -100,6 +102,8 @@ struct MsArgs {
   uint64_t* qe1;
   int32_t* tq;
   const int32_t* hubs;
+  const int32_t* unit_tile;  // bottom-up work unit u = tiles [unit_tile[u], unit_tile[u+1])
+  int64_t nunits;
   const uint32_t* hub_chunk;   // nhubs + 1 entries
   int64_t nhubs;
   DepthT* depth;             // [source][search-order vertex] rows, only reached entries written
@@ -707,7 +711,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
       // When most edge endpoints are frontier vertices, the fbits test
       // filters little and costs a load of its own: read fr[u] directly.
       const bool filter = 2 * E < (unsigned long long)a.m;
-      const int64_t ngroups = (a.W + kMsGrab - 1) / kMsGrab;
+      const int64_t ngroups = a.nunits;
       unsigned long long* next_unit = &c->tile_next[level % 3];
       for (;;) {
         // Work units from a level-wide counter: the hub chunks first, then
@@ -739,8 +743,10 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           mark(kPhHub);
           continue;
         }
-        const int64_t v_begin = ((int64_t)u0 - hub_chunks) * (kMsGrab << 5);
-        const int64_t v_stop = v_begin + (kMsGrab << 5) < a.n ? v_begin + (kMsGrab << 5) : a.n;
+        const int64_t unit = (int64_t)u0 - hub_chunks;
+        const int64_t v_begin = (int64_t)a.unit_tile[unit] << 5;
+        const int64_t v_end = (int64_t)a.unit_tile[unit + 1] << 5;
+        const int64_t v_stop = v_end < a.n ? v_end : a.n;
       for (int64_t v0 = v_begin; v0 < v_stop; v0 += 32) {
         const int64_t v = v0 + lane;
         LaneT vis = all;
