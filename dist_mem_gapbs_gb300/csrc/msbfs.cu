@@ -12,9 +12,9 @@
 // random then gather on a compact, cache-resident range, and tiles hold
 // vertices of similar degree.  This file builds that copy when the state is
 // first made, owns the buffers, captures one CUDA graph per batch buffer
-// (sources copy, buffer resets, the persistent cooperative kernel, the two
-// passes that put the depth rows back into original vertex order, a copy of
-// the control block back to the host), runs batches back to back with the
+// (sources copy, buffer resets, the persistent cooperative kernel, the pass
+// that writes the depth rows in original vertex order from the per-vertex
+// depth log, a copy of the control block back to the host), runs batches back to back with the
 // copy of one batch's depths overlapping the next batch, and holds the
 // autotuner.  Depth rows are uint8 (255 = unreached) or int32 (-1).
 
@@ -56,7 +56,10 @@ struct MsState {
   int32_t* perm = nullptr;           // original id -> search order id
   void* dtmp = nullptr;              // depth rows in search order (row stride dstride)
   int64_t dstride = 0;
-  void* drec = nullptr;              // per-vertex depth records, search order
+  uint32_t* lvl = nullptr;           // per-vertex depth log: levels, lane masks, flags
+  void* lmask = nullptr;
+  uint8_t* spill = nullptr;
+  uint32_t* tflag = nullptr;
   void* depth[2] = {nullptr, nullptr};
   int32_t* d_src[2] = {nullptr, nullptr};
   int32_t* h_src = nullptr;          // pinned, 2 x kMsMaxLanes
@@ -102,7 +105,10 @@ void msbfs_release(MsState* ms) {
   cudaFree(ms->rnbr);
   cudaFree(ms->perm);
   cudaFree(ms->dtmp);
-  cudaFree(ms->drec);
+  cudaFree(ms->lvl);
+  cudaFree(ms->lmask);
+  cudaFree(ms->spill);
+  cudaFree(ms->tflag);
   if (ms->h_src) cudaFreeHost(ms->h_src);
   if (ms->h_ctl) cudaFreeHost(ms->h_ctl);
   if (ms->ev0) cudaEventDestroy(ms->ev0);
@@ -117,13 +123,15 @@ void msbfs_release(MsState* ms) {
 // Lane words are allocated at 128 bits so every lane width fits: visit, the
 // two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
 // and tq; two frontier unions and the work-unit table; the search-ordered CSR (offsets counted at 8
-// bytes) and its permutation; depth rows of 128 sources in search order, the
-// same as per-vertex records, two buffers of rows in original order; slack
-// for the hub list and control blocks.
+// bytes) and its permutation; the per-vertex depth log (kLogSlots lane masks,
+// levels, flags); depth rows of 128 sources in search order for what the log
+// cannot hold and two buffers of rows in original order; slack for the hub
+// list and control blocks.
 size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes) {
   return 4 * 16 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 12 * (size_t)(W + 1) +
          8 * (size_t)(n + 1) + 4 * (size_t)m + 4 * (size_t)n +
-         4 * (size_t)kMsMaxLanes * (n + kDepthTile) * depth_bytes + (16 << 20);
+         (kLogSlots * sizeof(Lane128) + 9) * (size_t)n +
+         3 * (size_t)kMsMaxLanes * (n + kDepthTile) * depth_bytes + (16 << 20);
 }
 
 namespace {
@@ -311,7 +319,10 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
   ms->dstride = (n + kDepthTile - 1) / kDepthTile * kDepthTile;
   GB_TRY(alloc(&ms->dtmp, (size_t)kMsMaxLanes * ms->dstride * depth_bytes));
-  GB_TRY(alloc(&ms->drec, (size_t)kMsMaxLanes * n * depth_bytes));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->lvl), 4 * (size_t)n));
+  GB_TRY(alloc(&ms->lmask, (size_t)kLogSlots * sizeof(Lane128) * n));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->spill), (size_t)n));
+  GB_TRY(alloc(reinterpret_cast<void**>(&ms->tflag), 4 * (size_t)n));
   GB_TRY(g->off32 ? build_order<uint32_t>(g, ms, alloc)
                   : build_order<unsigned long long>(g, ms, alloc));
   for (int i = 0; i < 2; i++) {
@@ -372,6 +383,10 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.nhubs = ms->nhubs;
   a.depth = reinterpret_cast<DepthT*>(ms->dtmp);
   a.dstride = ms->dstride;
+  a.lvl = ms->lvl;
+  a.lmask = reinterpret_cast<LaneT*>(ms->lmask);
+  a.spill = ms->spill;
+  a.tflag = ms->tflag;
   a.sources = ms->d_src[buf];
   a.perm = ms->perm;
   a.ctl = ms->ctl[buf];
@@ -389,6 +404,9 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->visit, 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr[1], 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->acc, 0, lane_bytes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->lvl, 0xff, 4 * (size_t)g->n, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->spill, 0, (size_t)g->n, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ms->tflag, 0, 4 * (size_t)g->n, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->fbits[1], 0, 4 * (size_t)g->W, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->ctl[buf], 0, sizeof(MsCtl), s);
   if (e == cudaSuccess) {
@@ -409,12 +427,10 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   if (e == cudaSuccess) {
     constexpr int64_t kTileV = kDepthTile / (int64_t)sizeof(DepthT);
     const unsigned blocks = (unsigned)((g->n + kTileV - 1) / kTileV);
-    k_depth_records<LaneT, DepthT><<<blocks, kThreads, 0, s>>>(
-        reinterpret_cast<const DepthT*>(ms->dtmp), ms->dstride,
-        reinterpret_cast<const LaneT*>(ms->visit), reinterpret_cast<DepthT*>(ms->drec), g->n, k);
-    k_depth_gather<DepthT><<<blocks, kThreads, 0, s>>>(
-        reinterpret_cast<const DepthT*>(ms->drec), ms->perm,
-        reinterpret_cast<DepthT*>(ms->depth[buf]), g->n, k);
+    k_depth_decode<LaneT, DepthT><<<blocks, kThreads, 0, s>>>(
+        ms->lvl, reinterpret_cast<const LaneT*>(ms->lmask), ms->spill,
+        reinterpret_cast<const LaneT*>(ms->visit), reinterpret_cast<const DepthT*>(ms->dtmp),
+        ms->dstride, ms->perm, reinterpret_cast<DepthT*>(ms->depth[buf]), g->n, k);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)

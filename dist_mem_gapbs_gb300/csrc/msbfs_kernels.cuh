@@ -106,8 +106,12 @@ struct MsArgs {
   int64_t nunits;
   const uint32_t* hub_chunk;   // nhubs + 1 entries
   int64_t nhubs;
-  DepthT* depth;             // [source][search-order vertex] rows, only reached entries written
+  DepthT* depth;             // [source][search-order vertex] rows: entries the log cannot hold
   int64_t dstride;           // row stride of depth (elements, a multiple of kDepthTile)
+  uint32_t* lvl;             // per vertex: levels of its kLogSlots log entries (0xff = empty)
+  LaneT* lmask;              // per vertex: the lanes each log entry found
+  uint8_t* spill;            // per vertex: 1 if some depths are in the rows instead
+  uint32_t* tflag;           // per vertex: touched in this level (128-lane words)
   const int32_t* sources;   // original vertex ids
   const int32_t* perm;      // original id -> search order id
   MsCtl* ctl;
@@ -227,6 +231,40 @@ __device__ __forceinline__ bool first_or_lane(LaneT* p, LaneT v) {
   }
 }
 
+// OR nb into acc[v]; true for the one call per level that first touched v.
+// 32/64-lane words take it from the atomic's old value; a 128-lane word is
+// two 64-bit atomics, so there a per-vertex flag (cleared by the install)
+// decides instead.
+template <typename LaneT>
+__device__ __forceinline__ bool touch_or(LaneT* acc, uint32_t* tflag, int64_t v, LaneT nb) {
+  if constexpr (sizeof(LaneT) == 16) {
+    atomic_or_lane(acc + v, nb);
+    return atomicOr(tflag + v, 1u) == 0;
+  } else {
+    return first_or_lane(acc + v, nb);
+  }
+}
+
+// Per-vertex depth log: up to kLogSlots entries (level, lanes found at that
+// level).  A vertex is logged by one thread per level.  Returns true when
+// the entry does not fit (slots full, or a level above 254): the caller then
+// writes those depths into the rows and flags the vertex.
+constexpr int kLogSlots = 4;
+
+template <typename LaneT>
+__device__ __forceinline__ bool log_found(uint32_t* lvl, LaneT* lmask, int64_t v, LaneT nb,
+                                          int level) {
+  if (level > 254) return true;
+  const uint32_t w = __ldcg(lvl + v);
+  const uint32_t x = ~w;                                   // empty slots read 0x00
+  const uint32_t zero = (x - 0x01010101u) & ~x & 0x80808080u;
+  if (!zero) return true;
+  const int slot = (__ffs(zero) - 1) >> 3;                 // first empty slot
+  lmask[v * kLogSlots + slot] = nb;
+  lvl[v] = (w & ~(0xffu << (8 * slot))) | ((uint32_t)level << (8 * slot));
+  return false;
+}
+
 template <typename LaneT>
 __device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
   if constexpr (sizeof(LaneT) == 16) {
@@ -253,6 +291,10 @@ template <typename LaneT>
 __device__ __forceinline__ LaneT warp_or(LaneT x) {
   return group_or(kFull, x);
 }
+
+// Neighbour lists are read once per level: loads marked evict-first, so the
+// stream does not push the frontier words out of L2.
+__device__ __forceinline__ int32_t ld_stream(const int32_t* p) { return __ldcs(p); }
 
 // Frontier words and bits are read with L1-cached loads: they are written
 // only in the level before, and the acquire fence of the grid barrier in
@@ -403,7 +445,7 @@ __device__ __forceinline__ LaneT warp_gather_or(const int32_t* nbr, const uint32
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const uint64_t idx = e0 + 32 * r + lane;
-      u[r] = idx < e ? __ldg(nbr + idx) : -1;
+      u[r] = idx < e ? ld_stream(nbr + idx) : -1;
     }
     bool in[4];
 #pragma unroll
@@ -466,7 +508,8 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
     const int32_t s = a.perm[a.sources[i]];
     const LaneT bit = lane_bit<LaneT>(i);
     atomic_or_lane(a.visit + s, bit);
-    a.depth[(int64_t)i * a.dstride + s] = 0;
+    a.depth[(int64_t)i * a.dstride + s] = 0;   // depth 0 lives in the rows
+    a.spill[s] = 1;
     if (first_or_lane(a.fr1 + s, bit)) {
       const unsigned long long deg = (unsigned long long)(a.off[s + 1] - a.off[s]);
       if (deg) {
@@ -608,14 +651,14 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           bool first = false;
           int32_t v = 0;
           if (e < e_hi) {
-            v = __ldg(a.nbr + ob_s + (e - pre_s));
+            v = ld_stream(a.nbr + ob_s + (e - pre_s));
             if (dense) {
               // No visit test: the install pass masks visited bits anyway,
               // and the OR needs no result, so nothing waits on a load.
               atomic_or_lane(a.acc + v, f_s);
             } else {
               const LaneT nb = f_s & ~ld_lane(a.visit + v);
-              if (nb) first = first_or_lane(a.acc + v, nb);
+              if (nb) first = touch_or(a.acc, a.tflag, v, nb);
             }
           }
           if (!dense) warp_append(touched, a.tq, first, v);
@@ -650,7 +693,12 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           }
           const unsigned nm = __ballot_sync(kFull, nb != 0);
           if (lane == 0) fbn[v0 >> 5] = nm;
-          write_depths(a.depth, a.dstride, v, nb, level);
+          LaneT over = 0;
+          if (nb && log_found(a.lvl, a.lmask, v, nb, level)) {
+            over = nb;
+            a.spill[v] = 1;
+          }
+          write_depths(a.depth, a.dstride, v, over, level);
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
@@ -679,12 +727,16 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
             v = a.tq[i];
             nb = a.acc[v];
             a.acc[v] = 0;
+            a.tflag[v] = 0;
             const LaneT vis = a.visit[v];
             nb &= ~vis;
             if (nb) {
               a.visit[v] = vis | nb;
-              for (LaneT x = nb; x; x = clear_lowest(x))
-                a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
+              if (log_found(a.lvl, a.lmask, v, nb, level)) {
+                a.spill[v] = 1;
+                for (LaneT x = nb; x; x = clear_lowest(x))
+                  a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
+              }
               frn[v] = nb;
               atomicOr(fbn + (v >> 5), 1u << (v & 31));
               deg = (unsigned long long)(a.off[v + 1] - a.off[v]);
@@ -737,7 +789,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
             const LaneT got = warp_gather_or(a.nbr, fb, fr, b, e, vis, all, filter);
             const LaneT part = got & ~vis & all;
             bool first = false;
-            if (lane == 0 && part) first = first_or_lane(a.acc + v, part);
+            if (lane == 0 && part) first = touch_or(a.acc, a.tflag, v, part);
             warp_append(touched, a.tq, first, v);
           }
           mark(kPhHub);
@@ -782,7 +834,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           for (int r = 0; r < kR; r++) {
             const unsigned t = t0 + 32 * r + lane;
             o[r] = t < stotal ? own[t] : 32u;
-            u[r] = t < stotal ? __ldg(a.nbr + nbase[o[r]] + t) : -1;
+            u[r] = t < stotal ? ld_stream(a.nbr + nbase[o[r]] + t) : -1;
           }
           bool in[kR];
 #pragma unroll
@@ -813,7 +865,12 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
         if (v < a.n) frn[v] = nb;
         const unsigned nm = __ballot_sync(kFull, nb != 0);
         if (lane == 0 && (v0 >> 5) < a.W) fbn[v0 >> 5] = nm;
-        write_depths(a.depth, a.dstride, v, nb, level);
+        LaneT over = 0;
+        if (nb && log_found(a.lvl, a.lmask, v, nb, level)) {
+          over = nb;
+          a.spill[v] = 1;
+        }
+        write_depths(a.depth, a.dstride, v, over, level);
         if (nb) {
           my_count++;
           my_edges += deg;
@@ -845,12 +902,16 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
           const int32_t v = a.tq[i];
           LaneT nb = a.acc[v];
           a.acc[v] = 0;
+          a.tflag[v] = 0;
           const LaneT vis = a.visit[v];
           nb &= ~vis;
           if (nb) {
             a.visit[v] = vis | nb;
-            for (LaneT x = nb; x; x = clear_lowest(x))
-              a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
+            if (log_found(a.lvl, a.lmask, v, nb, level)) {
+              a.spill[v] = 1;
+              for (LaneT x = nb; x; x = clear_lowest(x))
+                a.depth[(int64_t)lowest_bit(x) * a.dstride + v] = (DepthT)level;
+            }
             frn[v] = nb;
             atomicOr(fbn + (v >> 5), 1u << (v & 31));
             atomicAdd(nf_count, 1ull);
@@ -907,104 +968,84 @@ __device__ __forceinline__ void transpose4x4(const uint32_t w[4], uint32_t r[4])
   r[3] = __byte_perm(hi01, hi23, 0x7632);
 }
 
-// Depth rows back to original vertex order, in two streaming passes.
-// k_depth_records: the search writes row i of source i in search order and
-// only at reached entries; a block turns kDepthTile bytes of every row into
-// one record of kMsMaxLanes depths per vertex (vertex-major), filling the
-// entries whose visit bit is clear with the unreached value, so the rows need
-// no reset before a batch.  k_depth_gather: a block fetches the records of
-// consecutive original vertices through perm (whole records, so
-// the random reads use every byte they move) and writes each row's segment
-// coalesced.  Both go through shared memory with padded rows; uint8 depths
-// move as 4x4 byte blocks.
-template <typename LaneT, typename DepthT>
-__global__ void __launch_bounds__(kThreads) k_depth_records(const DepthT* rows, int64_t stride,
-                                                            const LaneT* visit, DepthT* rec,
-                                                            int64_t n, int k) {
-  constexpr int kE = 16 / sizeof(DepthT);              // elements per 16-byte chunk
-  constexpr int kTileV = kDepthTile / (int)sizeof(DepthT);   // vertices per block
-  constexpr int kRowWords = kTileV * sizeof(DepthT) / 4 + 1;
-  __shared__ uint32_t tile[kMsMaxLanes * kRowWords];   // [row][vertex], padded rows
-  const int64_t p0 = (int64_t)blockIdx.x * kTileV;
-  constexpr int kChunks = kTileV / kE;             // chunks per row segment
-  for (int c = threadIdx.x; c < k * kChunks; c += blockDim.x) {
-    const int i = c / kChunks, j = c % kChunks;
-    const uint4 x = *reinterpret_cast<const uint4*>(rows + (int64_t)i * stride + p0 + j * kE);
-    uint32_t* t = tile + i * kRowWords + j * 4;
-    t[0] = x.x;
-    t[1] = x.y;
-    t[2] = x.z;
-    t[3] = x.w;
-  }
-  __syncthreads();
-  if constexpr (sizeof(DepthT) == 1) {
-    // 4 rows x 4 vertices per step: a word of each row, transposed into a
-    // word of each vertex's record; entries not reached become 0xff.
-    constexpr int kGroups = kMsMaxLanes / 4;
-    for (int t = threadIdx.x; t < kGroups * (kTileV / 4); t += blockDim.x) {
-      const int a4 = t % kGroups, b4 = t / kGroups;
-      uint32_t w[4], r[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int i = 4 * a4 + j;
-        w[j] = i < k ? tile[i * kRowWords + b4] : 0xffffffffu;
-      }
-      transpose4x4(w, r);
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int64_t p = p0 + 4 * b4 + j;
-        if (p >= n) break;
-        uint32_t bits = 0;
-        if (4 * a4 < (int)(8 * sizeof(LaneT)))
-          bits = (word32(visit[p], a4 >> 3) >> (4 * (a4 & 7))) & 0xfu;
-        if (4 * a4 + 4 > k) bits &= (k > 4 * a4) ? ((1u << (k - 4 * a4)) - 1) : 0u;
-        const uint32_t m = ((bits * 0x204081u) & 0x01010101u) * 0xffu;
-        reinterpret_cast<uint32_t*>(rec + p * kMsMaxLanes)[a4] = (r[j] & m) | ~m;
-      }
-    }
-  } else {
-    constexpr int kRecChunks = kMsMaxLanes / kE;       // chunks per record
-    const DepthT* tb = reinterpret_cast<const DepthT*>(tile);
-    for (int t = threadIdx.x; t < kTileV * kRecChunks; t += blockDim.x) {
-      const int q = t / kRecChunks, c = t % kRecChunks;
-      const int64_t p = p0 + q;
-      if (p >= n) continue;
-      const LaneT vis = visit[p];
-      uint32_t w[4];
-      DepthT* e = reinterpret_cast<DepthT*>(w);
-#pragma unroll
-      for (int r = 0; r < kE; r++) {
-        const int i = c * kE + r;
-        const bool hit = i < k && i < (int)(8 * sizeof(LaneT)) && lane_test(vis, i);
-        e[r] = hit ? tb[(int64_t)i * kRowWords * (4 / sizeof(DepthT)) + q] : (DepthT)-1;
-      }
-      *reinterpret_cast<uint4*>(rec + p * kMsMaxLanes + c * kE) =
-          make_uint4(w[0], w[1], w[2], w[3]);
-    }
-  }
+// Bits 0..7 of x to bits 0, 4, ..., 28 (nibble spacing).
+__device__ __forceinline__ uint32_t spread_byte(uint32_t x) {
+  x = (x | (x << 12)) & 0x000f000fu;
+  x = (x | (x << 6)) & 0x03030303u;
+  return (x | (x << 3)) & 0x11111111u;
 }
 
-template <typename DepthT>
-__global__ void __launch_bounds__(kThreads) k_depth_gather(const DepthT* rec, const int32_t* perm,
-                                                           DepthT* out, int64_t n, int k) {
-  constexpr int kE = 16 / sizeof(DepthT);
+// Depth rows in original vertex order from the per-vertex logs.  A block
+// takes kTileV consecutive original vertices, reads each one's log through
+// perm (a few contiguous words), builds its record of depths in shared
+// memory, and then writes every row's segment coalesced (uint8 rows as 4x4
+// byte blocks).  For uint8, 4 lanes' depths come from one __byte_perm of the
+// log's level word: the selector nibble of a lane is the index of the log
+// entry holding it (bit planes b0 = entry 1 or 3, b1 = entry 2 or 3,
+// b2 = none, which selects 0xff).  Lanes of a flagged vertex that the log
+// does not hold but visit has are read from the rows.
+template <typename LaneT, typename DepthT>
+__global__ void __launch_bounds__(kThreads) k_depth_decode(
+    const uint32_t* lvl, const LaneT* lmask, const uint8_t* spill, const LaneT* visit,
+    const DepthT* rows, int64_t stride, const int32_t* perm, DepthT* out, int64_t n, int k) {
   constexpr int kTileV = kDepthTile / (int)sizeof(DepthT);   // vertices per block
   constexpr int kRecWords = kMsMaxLanes * sizeof(DepthT) / 4 + 1;
   __shared__ uint32_t tile[kTileV * kRecWords];    // [vertex][row], padded records
   const int64_t v0 = (int64_t)blockIdx.x * kTileV;
-  constexpr int kRecChunks = kMsMaxLanes / kE;
-  const int used = (k + kE - 1) / kE;                  // chunks holding rows < k
-  for (int t = threadIdx.x; t < kTileV * kRecChunks; t += blockDim.x) {
-    const int q = t / kRecChunks, c = t % kRecChunks;
-    const int64_t v = v0 + q;
-    if (v >= n || c >= used) continue;
-    const int64_t p = perm[v];
-    const uint4 x = *reinterpret_cast<const uint4*>(rec + p * kMsMaxLanes + c * kE);
-    uint32_t* d = tile + q * kRecWords + c * 4;
-    d[0] = x.x;
-    d[1] = x.y;
-    d[2] = x.z;
-    d[3] = x.w;
+  if constexpr (sizeof(DepthT) == 1) {
+    const int words = (k + 31) / 32;                 // 32-lane words of the lane word in use
+    for (int t = threadIdx.x; t < kTileV * words; t += blockDim.x) {
+      const int q = t / words, h = t % words;
+      const int64_t v = v0 + q;
+      if (v >= n) continue;
+      const int64_t p = perm[v];
+      const uint32_t lw = lvl[p];
+      uint32_t W[kLogSlots];
+#pragma unroll
+      for (int j = 0; j < kLogSlots; j++)
+        W[j] = ((lw >> (8 * j)) & 0xffu) != 0xffu ? word32(lmask[p * kLogSlots + j], h) : 0u;
+      const uint32_t reach = W[0] | W[1] | W[2] | W[3];
+      const uint32_t b0 = W[1] | W[3], b1 = W[2] | W[3], b2 = ~reach;
+      uint32_t sel[4];
+#pragma unroll
+      for (int y = 0; y < 4; y++)
+        sel[y] = spread_byte((b0 >> (8 * y)) & 0xffu) | (spread_byte((b1 >> (8 * y)) & 0xffu) << 1) |
+                 (spread_byte((b2 >> (8 * y)) & 0xffu) << 2);
+      const uint32_t extra = spill[p] ? word32(visit[p], h) & ~reach : 0u;
+      uint32_t* rec = tile + q * kRecWords + 8 * h;
+#pragma unroll
+      for (int g = 0; g < 8; g++) {
+        uint32_t d = __byte_perm(lw, 0xffffffffu, (sel[g >> 1] >> (16 * (g & 1))) & 0xffffu);
+        for (uint32_t e = (extra >> (4 * g)) & 0xfu; e; e &= e - 1) {
+          const int r = __ffs(e) - 1;
+          const int i = 32 * h + 4 * g + r;
+          const uint32_t b = (uint8_t)rows[(int64_t)i * stride + p];
+          d = (d & ~(0xffu << (8 * r))) | (b << (8 * r));
+        }
+        rec[g] = d;
+      }
+    }
+  } else {
+    for (int t = threadIdx.x; t < kTileV * k; t += blockDim.x) {
+      const int q = t / k, i = t % k;
+      const int64_t v = v0 + q;
+      if (v >= n) continue;
+      const int64_t p = perm[v];
+      const uint32_t lw = lvl[p];
+      DepthT d = (DepthT)-1;
+      bool found = false;
+      for (int j = 0; j < kLogSlots; j++) {
+        const uint32_t L = (lw >> (8 * j)) & 0xffu;
+        if (L == 0xffu) break;
+        if (lane_test(lmask[p * kLogSlots + j], i)) {
+          d = (DepthT)L;
+          found = true;
+          break;
+        }
+      }
+      if (!found && spill[p] && lane_test(visit[p], i)) d = rows[(int64_t)i * stride + p];
+      tile[q * kRecWords + i] = (uint32_t)d;
+    }
   }
   __syncthreads();
   if constexpr (sizeof(DepthT) == 1) {
