@@ -425,7 +425,7 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
     e = cudaLaunchKernelExC(&lc, fn, args);
   }
   if (e == cudaSuccess) {
-    constexpr int64_t kTileV = kDepthTile / (int64_t)sizeof(DepthT);
+    constexpr int64_t kTileV = kDecodeTile / (int64_t)sizeof(DepthT);
     const unsigned blocks = (unsigned)((g->n + kTileV - 1) / kTileV);
     k_depth_decode<LaneT, DepthT><<<blocks, kThreads, 0, s>>>(
         ms->lvl, reinterpret_cast<const LaneT*>(ms->lmask), ms->spill,

@@ -59,7 +59,8 @@ constexpr int kMsSmall = 32;        // bottom-up: lower degrees share a streamed
 #define GBBFS_MS_ORDER_DEG 1
 #endif
 constexpr int kMsOrderDeg = GBBFS_MS_ORDER_DEG;
-constexpr int kDepthTile = 128;     // bytes of each row per block of the depth record passes
+constexpr int kDepthTile = 128;     // rows in search order: stride a multiple of this
+constexpr int kDecodeTile = 64;     // bytes of each row per block of the depth decode
 constexpr int kMsMaxLanes = 128;    // sources per batch at most (depth record length)
 constexpr int kMsGrab = 8;          // tiles of 32 vertices in a bottom-up work unit at most
 constexpr int kMsUnitEdges = 4096;  // a unit also ends once its tiles hold this many edges
@@ -988,7 +989,7 @@ template <typename LaneT, typename DepthT>
 __global__ void __launch_bounds__(kThreads) k_depth_decode(
     const uint32_t* lvl, const LaneT* lmask, const uint8_t* spill, const LaneT* visit,
     const DepthT* rows, int64_t stride, const int32_t* perm, DepthT* out, int64_t n, int k) {
-  constexpr int kTileV = kDepthTile / (int)sizeof(DepthT);   // vertices per block
+  constexpr int kTileV = kDecodeTile / (int)sizeof(DepthT);  // vertices per block
   constexpr int kRecWords = kMsMaxLanes * sizeof(DepthT) / 4 + 1;
   __shared__ uint32_t tile[kTileV * kRecWords];    // [vertex][row], padded records
   const int64_t v0 = (int64_t)blockIdx.x * kTileV;
@@ -999,11 +1000,16 @@ __global__ void __launch_bounds__(kThreads) k_depth_decode(
       const int64_t v = v0 + q;
       if (v >= n) continue;
       const int64_t p = perm[v];
+      // Every slot's mask is loaded with the level word (unused slots are
+      // masked out after), so only perm -> log is a dependent chain.
       const uint32_t lw = lvl[p];
       uint32_t W[kLogSlots];
 #pragma unroll
       for (int j = 0; j < kLogSlots; j++)
-        W[j] = ((lw >> (8 * j)) & 0xffu) != 0xffu ? word32(lmask[p * kLogSlots + j], h) : 0u;
+        W[j] = reinterpret_cast<const uint32_t*>(lmask + p * kLogSlots + j)[h];
+#pragma unroll
+      for (int j = 0; j < kLogSlots; j++)
+        if (((lw >> (8 * j)) & 0xffu) == 0xffu) W[j] = 0u;
       const uint32_t reach = W[0] | W[1] | W[2] | W[3];
       const uint32_t b0 = W[1] | W[3], b1 = W[2] | W[3], b2 = ~reach;
       uint32_t sel[4];
