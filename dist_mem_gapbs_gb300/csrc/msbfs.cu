@@ -29,6 +29,8 @@
 
 namespace gbbfs {
 
+constexpr int kSrcSlot = kMsMaxLanes + 1;   // per batch buffer: count, then the sources
+
 struct MsConfig {
   int lanes = 64;        // 32, 64 or 128 sources per batch
   int batch = 8;         // neighbours per bottom-up round of one thread
@@ -62,18 +64,18 @@ struct MsState {
   uint32_t* tflag = nullptr;
   void* depth[2] = {nullptr, nullptr};
   int32_t* d_src[2] = {nullptr, nullptr};
-  int32_t* h_src = nullptr;          // pinned, 2 x kMsMaxLanes
+  int32_t* h_src = nullptr;          // pinned, 2 x kSrcSlot: count, then the sources
   MsCtl* ctl[2] = {nullptr, nullptr};
   MsCtl* h_ctl = nullptr;            // pinned, 2
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t computed[2] = {nullptr, nullptr};
   cudaEvent_t copied[2] = {nullptr, nullptr};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  // One captured graph per batch buffer and lane width (32, 64, 128); the
+  // source count is read on the device, so a graph serves every batch size.
+  cudaGraphExec_t exec[2][3] = {};
+  MsConfig exec_cfg[2][3];
   MsConfig cfg;
-  MsConfig exec_cfg;
-  int exec_k[2] = {-1, -1};
-  int grid = 0;
   int64_t bytes = 0;
   int last_buf = -1;
   int last_k = 0;
@@ -82,7 +84,8 @@ struct MsState {
 void msbfs_release(MsState* ms) {
   if (!ms) return;
   for (int i = 0; i < 2; i++) {
-    if (ms->exec[i]) cudaGraphExecDestroy(ms->exec[i]);
+    for (int c = 0; c < 3; c++)
+      if (ms->exec[i][c]) cudaGraphExecDestroy(ms->exec[i][c]);
     cudaFree(ms->q[i]);
     cudaFree(ms->qe[i]);
     cudaFree(ms->depth[i]);
@@ -329,12 +332,12 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->q[i]), 4 * (size_t)n));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->qe[i]), 8 * (size_t)n));
     GB_TRY(alloc(&ms->depth[i], (size_t)kMsMaxLanes * n * depth_bytes));
-    GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), kMsMaxLanes * sizeof(int32_t)));
+    GB_TRY(alloc(reinterpret_cast<void**>(&ms->d_src[i]), kSrcSlot * sizeof(int32_t)));
     GB_TRY(alloc(reinterpret_cast<void**>(&ms->ctl[i]), sizeof(MsCtl)));
     GB_CUDA(cudaEventCreateWithFlags(&ms->computed[i], cudaEventDisableTiming));
     GB_CUDA(cudaEventCreateWithFlags(&ms->copied[i], cudaEventDisableTiming));
   }
-  GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_src), 2 * kMsMaxLanes * sizeof(int32_t),
+  GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_src), 2 * kSrcSlot * sizeof(int32_t),
                         cudaHostAllocDefault));
   GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ms->h_ctl), 2 * sizeof(MsCtl),
                         cudaHostAllocDefault));
@@ -348,9 +351,10 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
 }
 
 template <typename OffT, typename LaneT, typename DepthT>
-int capture_batch(gbbfs_graph* g, int buf, int k) {
+int capture_batch(gbbfs_graph* g, int buf, int cls) {
   MsState* ms = g->ms;
-  const MsConfig& cfg = ms->cfg;
+  MsConfig cfg = ms->cfg;
+  cfg.lanes = 32 << cls;
   const void* fn = kernel_for(g, cfg, (int)sizeof(DepthT));
   int per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
@@ -358,7 +362,7 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
     ms_error = "multi-source kernel does not fit on an SM";
     return GBBFS_ERR_CUDA;
   }
-  ms->grid = per_sm * g->sms;
+  const int grid = per_sm * g->sms;
   MsArgs<OffT, LaneT, DepthT> a;
   a.off = reinterpret_cast<const OffT*>(ms->roff);
   a.nbr = ms->rnbr;
@@ -387,10 +391,10 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   a.lmask = reinterpret_cast<LaneT*>(ms->lmask);
   a.spill = ms->spill;
   a.tflag = ms->tflag;
-  a.sources = ms->d_src[buf];
+  a.nsrc = ms->d_src[buf];
+  a.sources = ms->d_src[buf] + 1;
   a.perm = ms->perm;
   a.ctl = ms->ctl[buf];
-  a.k = k;
   a.shift = g->shift;
   a.alpha = std::max(1, cfg.alpha);
   a.limit_ns = 5ull * 1000 * 1000 * 1000;  // 5 s per barrier
@@ -398,9 +402,8 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   cudaStream_t s = g->stream;
   const size_t lane_bytes = sizeof(LaneT) * (size_t)g->n;
   GB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = cudaMemcpyAsync(ms->d_src[buf], ms->h_src + kMsMaxLanes * buf,
-                                  kMsMaxLanes * sizeof(int32_t),
-                                  cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaMemcpyAsync(ms->d_src[buf], ms->h_src + kSrcSlot * buf,
+                                  kSrcSlot * sizeof(int32_t), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->visit, 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->fr[1], 0, lane_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ms->acc, 0, lane_bytes, s);
@@ -412,7 +415,7 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   if (e == cudaSuccess) {
     cudaLaunchConfig_t lc;
     memset(&lc, 0, sizeof lc);
-    lc.gridDim = dim3(ms->grid);
+    lc.gridDim = dim3(grid);
     lc.blockDim = dim3(kThreads);
     lc.dynamicSmemBytes = 0;
     lc.stream = s;
@@ -430,7 +433,7 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
     k_depth_decode<LaneT, DepthT><<<blocks, kThreads, 0, s>>>(
         ms->lvl, reinterpret_cast<const LaneT*>(ms->lmask), ms->spill,
         reinterpret_cast<const LaneT*>(ms->visit), reinterpret_cast<const DepthT*>(ms->dtmp),
-        ms->dstride, ms->perm, reinterpret_cast<DepthT*>(ms->depth[buf]), g->n, k);
+        ms->dstride, ms->perm, reinterpret_cast<DepthT*>(ms->depth[buf]), g->n, ms->d_src[buf]);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)
@@ -439,31 +442,30 @@ int capture_batch(gbbfs_graph* g, int buf, int k) {
   cudaError_t e2 = cudaStreamEndCapture(s, &graph);
   if (e == cudaSuccess) e = e2;
   if (e == cudaSuccess) {
-    if (ms->exec[buf]) cudaGraphExecDestroy(ms->exec[buf]);
-    ms->exec[buf] = nullptr;
-    e = cudaGraphInstantiate(&ms->exec[buf], graph, 0);
+    if (ms->exec[buf][cls]) cudaGraphExecDestroy(ms->exec[buf][cls]);
+    ms->exec[buf][cls] = nullptr;
+    e = cudaGraphInstantiate(&ms->exec[buf][cls], graph, 0);
   }
   if (graph) cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
     ms_error = std::string("multi-source graph capture: ") + cudaGetErrorString(e);
     return GBBFS_ERR_CUDA;
   }
-  ms->exec_k[buf] = k;
-  ms->exec_cfg = cfg;
+  ms->exec_cfg[buf][cls] = cfg;
   return GBBFS_OK;
 }
 
 template <typename OffT, typename LaneT>
-int capture_depth(gbbfs_graph* g, int buf, int k) {
-  return g->ms->depth_bytes == 1 ? capture_batch<OffT, LaneT, uint8_t>(g, buf, k)
-                                 : capture_batch<OffT, LaneT, int32_t>(g, buf, k);
+int capture_depth(gbbfs_graph* g, int buf, int cls) {
+  return g->ms->depth_bytes == 1 ? capture_batch<OffT, LaneT, uint8_t>(g, buf, cls)
+                                 : capture_batch<OffT, LaneT, int32_t>(g, buf, cls);
 }
 
 template <typename OffT>
-int capture_lanes(gbbfs_graph* g, int buf, int k) {
-  if (g->ms->cfg.lanes == 128) return capture_depth<OffT, Lane128>(g, buf, k);
-  return g->ms->cfg.lanes == 32 ? capture_depth<OffT, uint32_t>(g, buf, k)
-                                : capture_depth<OffT, unsigned long long>(g, buf, k);
+int capture_lanes(gbbfs_graph* g, int buf, int cls) {
+  if (cls == 2) return capture_depth<OffT, Lane128>(g, buf, cls);
+  return cls == 0 ? capture_depth<OffT, uint32_t>(g, buf, cls)
+                  : capture_depth<OffT, unsigned long long>(g, buf, cls);
 }
 
 bool same_cfg(const MsConfig& a, const MsConfig& b) {
@@ -479,19 +481,27 @@ int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
       return GBBFS_ERR_ARG;
     }
   }
+  // The narrowest lane word that holds the batch (never wider than the
+  // configured one): a small batch costs a 32-lane search.
+  int cls = 0;
+  while ((32 << cls) < k) cls++;
+  MsConfig want = ms->cfg;
+  want.lanes = 32 << cls;
   // The buffer's previous results must have left the device first.
   GB_CUDA(cudaStreamWaitEvent(g->stream, ms->copied[buf], 0));
-  if (!ms->exec[buf] || ms->exec_k[buf] != k || !same_cfg(ms->exec_cfg, ms->cfg)) {
+  if (!ms->exec[buf][cls] || !same_cfg(ms->exec_cfg[buf][cls], want)) {
     GB_CUDA(cudaStreamSynchronize(g->stream));
-    int rc = g->off32 ? capture_lanes<uint32_t>(g, buf, k)
-                      : capture_lanes<unsigned long long>(g, buf, k);
+    int rc = g->off32 ? capture_lanes<uint32_t>(g, buf, cls)
+                      : capture_lanes<unsigned long long>(g, buf, cls);
     if (rc != GBBFS_OK) return rc;
   }
   // The host copy of the sources is read by the graph's first node; wait
   // until the previous launch that read this slot is done.
   GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
-  memcpy(ms->h_src + kMsMaxLanes * buf, sources, sizeof(int32_t) * k);
-  GB_CUDA(cudaGraphLaunch(ms->exec[buf], g->stream));
+  int32_t* slot = ms->h_src + kSrcSlot * buf;
+  slot[0] = k;
+  memcpy(slot + 1, sources, sizeof(int32_t) * k);
+  GB_CUDA(cudaGraphLaunch(ms->exec[buf][cls], g->stream));
   GB_CUDA(cudaEventRecord(ms->computed[buf], g->stream));
   return GBBFS_OK;
 }

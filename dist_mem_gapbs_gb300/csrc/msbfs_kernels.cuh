@@ -113,10 +113,10 @@ struct MsArgs {
   LaneT* lmask;              // per vertex: the lanes each log entry found
   uint8_t* spill;            // per vertex: 1 if some depths are in the rows instead
   uint32_t* tflag;           // per vertex: touched in this level (128-lane words)
+  const int32_t* nsrc;      // sources in this batch (device, set per launch)
   const int32_t* sources;   // original vertex ids
   const int32_t* perm;      // original id -> search order id
   MsCtl* ctl;
-  int k;
   int shift;
   int alpha;
   unsigned long long limit_ns;
@@ -481,7 +481,8 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
   const int64_t warp = tid >> 5;
   const int64_t nwarps = nthreads >> 5;
   const unsigned long long emask = (1ull << a.shift) - 1;
-  const LaneT all = lane_ones<LaneT>(a.k);
+  const int k = *a.nsrc;
+  const LaneT all = lane_ones<LaneT>(k);
   const int max_level = sizeof(DepthT) == 1 ? 254 : 0x7ffffffe;
   const int64_t hub_chunks = a.nhubs ? (int64_t)a.hub_chunk[a.nhubs] : 0;
   if (tid == 0) c->t_begin = globaltimer();
@@ -504,7 +505,7 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
 
   // Level 1's frontier: lane i starts at sources[i] with depth 0.  A vertex
   // that is the source of several lanes is queued once.
-  if (blockIdx.x == 0 && threadIdx.x < a.k) {
+  if (blockIdx.x == 0 && threadIdx.x < k) {
     const int i = threadIdx.x;
     const int32_t s = a.perm[a.sources[i]];
     const LaneT bit = lane_bit<LaneT>(i);
@@ -988,7 +989,9 @@ __device__ __forceinline__ uint32_t spread_byte(uint32_t x) {
 template <typename LaneT, typename DepthT>
 __global__ void __launch_bounds__(kThreads) k_depth_decode(
     const uint32_t* lvl, const LaneT* lmask, const uint8_t* spill, const LaneT* visit,
-    const DepthT* rows, int64_t stride, const int32_t* perm, DepthT* out, int64_t n, int k) {
+    const DepthT* rows, int64_t stride, const int32_t* perm, DepthT* out, int64_t n,
+    const int32_t* nsrc) {
+  const int k = *nsrc;
   constexpr int kTileV = kDecodeTile / (int)sizeof(DepthT);  // vertices per block
   constexpr int kRecWords = kMsMaxLanes * sizeof(DepthT) / 4 + 1;
   __shared__ uint32_t tile[kTileV * kRecWords];    // [vertex][row], padded records
