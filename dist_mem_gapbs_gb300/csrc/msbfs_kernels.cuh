@@ -64,7 +64,7 @@ constexpr int kDecodeTile = 64;     // bytes of each row per block of the depth 
 constexpr int kMsMaxLanes = 128;    // sources per batch at most (depth record length)
 constexpr int kMsGrab = 8;          // tiles of 32 vertices in a bottom-up work unit at most
 constexpr int kMsUnitEdges = 4096;  // a unit also ends once its tiles hold this many edges
-constexpr int kMsHubDeg = 2048;
+constexpr int kMsHubDeg = 4096;
 constexpr int kMsHubChunk = 2048;
 constexpr int kMsTdSpan = 2048;     // edges per warp span of a top-down level
 
