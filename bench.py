@@ -325,16 +325,18 @@ def run_gbbfs(args):
     achieved = kind_bytes[dom] / kind_time[dom] / 1e9 if kind_time[dom] > 0 else 0.0
     traffic = load_traffic(args.graph, kernel_names[dom])
 
-    # End to end through the public call: source in, parent array back in
-    # pinned host memory, every search.
+    # End to end through the public call: the sources in, every search's
+    # parent array back in pinned host memory (gbbfs_bfs_many: each copy runs
+    # while the next search does).  Each search is charged an equal share of
+    # the call's wall time.
     pinned = torch.empty(n, dtype=torch.int32, pin_memory=True)
     host_parent = pinned.numpy()
-    e2e_secs, e2e_edges = [], []
-    for s in sources:
-        t1 = time.perf_counter()
-        gbbfs.DOBFS(g, s, parent_out=host_parent)
-        e2e_secs.append(time.perf_counter() - t1)
-        e2e_edges.append(info[s]["edges"])
+    gbbfs.bfs_many(g, sources[:2], host_parent)          # staging arrays allocated
+    t1 = time.perf_counter()
+    gbbfs.bfs_many(g, sources, host_parent)
+    e2e_wall = time.perf_counter() - t1
+    e2e_edges = [info[s]["edges"] for s in sources]
+    e2e_secs = [e2e_wall / len(sources)] * len(sources)
     e2e_value = hmean_gteps(e2e_edges, e2e_secs)
 
     if tdist is not None:

@@ -59,6 +59,13 @@ void release(gbbfs_graph* g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   msbfs_release(g->ms);
   g->ms = nullptr;
+  if (g->copy_stream) cudaStreamSynchronize(g->copy_stream);
+  for (int i = 0; i < 2; i++) {
+    cudaFree(g->stage[i]);
+    if (g->staged[i]) cudaEventDestroy(g->staged[i]);
+    if (g->copied[i]) cudaEventDestroy(g->copied[i]);
+  }
+  if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->off);
@@ -543,6 +550,45 @@ int gbbfs_bfs(gbbfs_graph* g, int32_t source, int alpha, int beta, int32_t* pare
   int rc = search(g, source, alpha, beta, depth_out != nullptr, st);
   if (rc != GBBFS_OK) return rc;
   return gbbfs_results(g, parent_out, depth_out);
+}
+
+int gbbfs_bfs_many(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha, int beta,
+                   int32_t* const* parent_out, gbbfs_stats* st) {
+  if (!g || k < 0 || (k > 0 && (!sources || !parent_out))) return GBBFS_ERR_ARG;
+  for (int64_t i = 0; i < k; i++)
+    if (!parent_out[i]) return GBBFS_ERR_ARG;
+  GB_CUDA(cudaSetDevice(g->device));
+  if (!g->copy_stream) {
+    for (int i = 0; i < 2; i++) {
+      cudaError_t e = cudaMalloc(&g->stage[i], sizeof(int32_t) * (size_t)g->n);
+      if (e != cudaSuccess) {
+        g_last_error = std::string("staging arrays: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? GBBFS_ERR_NOMEM : GBBFS_ERR_CUDA;
+      }
+      g->device_bytes += (int64_t)sizeof(int32_t) * g->n;
+      GB_CUDA(cudaEventCreateWithFlags(&g->staged[i], cudaEventDisableTiming));
+      GB_CUDA(cudaEventCreateWithFlags(&g->copied[i], cudaEventDisableTiming));
+    }
+    GB_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+  }
+  const size_t bytes = sizeof(int32_t) * (size_t)g->n;
+  int rc = GBBFS_OK;
+  for (int64_t i = 0; i < k && rc == GBBFS_OK; i++) {
+    const int b = (int)(i & 1);
+    // staging array b is free once the copy of search i-2 has left it
+    GB_CUDA(cudaStreamWaitEvent(g->stream, g->copied[b], 0));
+    rc = search(g, sources[i], alpha, beta, false, st ? st + i : nullptr);
+    if (rc != GBBFS_OK) break;
+    GB_CUDA(cudaMemcpyAsync(g->stage[b], g->parent, bytes, cudaMemcpyDeviceToDevice, g->stream));
+    GB_CUDA(cudaEventRecord(g->staged[b], g->stream));
+    GB_CUDA(cudaStreamWaitEvent(g->copy_stream, g->staged[b], 0));
+    GB_CUDA(cudaMemcpyAsync(parent_out[i], g->stage[b], bytes, cudaMemcpyDeviceToHost,
+                            g->copy_stream));
+    GB_CUDA(cudaEventRecord(g->copied[b], g->copy_stream));
+  }
+  GB_CUDA(cudaStreamSynchronize(g->copy_stream));
+  GB_CUDA(cudaStreamSynchronize(g->stream));
+  return rc;
 }
 
 }  // extern "C"

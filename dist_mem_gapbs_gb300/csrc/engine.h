@@ -88,4 +88,9 @@ struct gbbfs_graph {
   bool have_result = false;
   bool result_depth = false;
   gbbfs::MsState* ms = nullptr;
+  // gbbfs_bfs_many: staged parent arrays and their copy-out stream.
+  int32_t* stage[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t staged[2] = {nullptr, nullptr};
+  cudaEvent_t copied[2] = {nullptr, nullptr};
 };

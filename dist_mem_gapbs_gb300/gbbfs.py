@@ -29,6 +29,7 @@ STEP_NAME = {STEP_TD: "td", STEP_E: "e", STEP_BU: "bu", STEP_C: "c"}
 # Every symbol include/gbbfs.h declares (the tests check the library exports them).
 EXPORTS = (
     "gbbfs_graph_create", "gbbfs_graph_destroy", "gbbfs_graph_info", "gbbfs_bfs",
+    "gbbfs_bfs_many",
     "gbbfs_bfs_device", "gbbfs_results", "gbbfs_result_device_ptrs", "gbbfs_strerror",
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
@@ -114,6 +115,7 @@ def lib():
             "gbbfs_graph_destroy": (I, [P]),
             "gbbfs_graph_info": (I, [P, P, P, P]),
             "gbbfs_bfs": (I, [P, i32, I, I, P, P, P]),
+            "gbbfs_bfs_many": (I, [P, P, i64, I, I, P, P]),
             "gbbfs_bfs_device": (I, [P, i32, I, I, I, P]),
             "gbbfs_results": (I, [P, P, P]),
             "gbbfs_result_device_ptrs": (I, [P, PP, PP]),
@@ -339,6 +341,28 @@ def DOBFS(g, source, alpha=15, beta=18, depth=False, stats=False, instrument=Fal
     if st is not None:
         out.append(SearchStats(st, steps))
     return out[0] if len(out) == 1 else tuple(out)
+
+
+def bfs_many(g, sources, out, alpha=15, beta=18):
+    """Searches from every source back to back, each parent array copied to
+    host memory while the next search runs.  `out` is a (k, n) int32 array
+    (row i for sources[i]) or one n-entry array that every search overwrites
+    in turn (the last source's parents remain)."""
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    k = len(src)
+    if out.dtype != np.int32 or not out.flags["C_CONTIGUOUS"]:
+        raise ValueError("out must be a contiguous int32 array")
+    if out.ndim == 2:
+        if out.shape != (k, g.n):
+            raise ValueError("out must be (len(sources), n)")
+        ptrs = (ctypes.c_void_p * max(k, 1))(*[out[i].ctypes.data for i in range(k)])
+    else:
+        if out.shape != (g.n,):
+            raise ValueError("out must have n entries")
+        ptrs = (ctypes.c_void_p * max(k, 1))(*([out.ctypes.data] * k))
+    _check(lib().gbbfs_bfs_many(g.handle, _p(src), k, int(alpha), int(beta), ptrs, None),
+           "bfs_many")
+    return out
 
 
 def bfs_device(g, source, alpha=15, beta=18, want_depth=False, stats=False, instrument=False,

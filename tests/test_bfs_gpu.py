@@ -181,6 +181,29 @@ def test_repeated_searches_reuse_state(native, oracle):
         assert e.value.status == native.ERR_STATE
 
 
+def test_many_searches_pipelined(native, oracle):
+    """gbbfs_bfs_many: the trial loop in one call, each parent array copied
+    out while the next search runs.  Every row is a valid BFS tree of its own
+    source (rows in source order), and one shared output keeps the last."""
+    off, nbr = native.make_graph(16, 16, False)
+    with native.Graph(off, nbr) as g:
+        srcs = native.pick_sources(off, 7)
+        out = np.full((len(srcs), g.n), -7, np.int32)
+        native.bfs_many(g, srcs, out)
+        for i, s in enumerate(srcs):
+            ok, why = oracle.verify(off, nbr, int(s), out[i])
+            assert ok, (i, why)
+            assert out[i][int(s)] == int(s)
+        one = np.full(g.n, -7, np.int32)
+        native.bfs_many(g, srcs[::-1], one)
+        ok, why = oracle.verify(off, nbr, int(srcs[0]), one)
+        assert ok, why
+        native.bfs_many(g, srcs[:0], one)
+        with pytest.raises(native.GbbfsError):
+            native.bfs_many(g, np.array([srcs[0], g.n + 2], np.int32),
+                            np.empty((2, g.n), np.int32))
+
+
 def test_offset64_path(native, oracle, golden, monkeypatch):
     """The uint64-offset kernels (graphs with >= 2^32 directed edges), forced
     onto small graphs."""
