@@ -32,7 +32,7 @@ namespace gbbfs {
 constexpr int kSrcSlot = kMsMaxLanes + 1;   // per batch buffer: count, then the sources
 
 struct MsConfig {
-  int lanes = 64;        // 32, 64 or 128 sources per batch
+  int lanes = 128;       // 32, 64 or 128 sources per batch (the widest used)
   int batch = 8;         // neighbours per bottom-up round of one thread
   int alpha = 15;        // top-down while frontier degrees <= m / alpha
 };

@@ -348,9 +348,9 @@ int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out) {
   gbbfs_server* s = new (std::nothrow) gbbfs_server();
   if (!s) return GBBFS_ERR_NOMEM;
   memset(&s->cfg, 0, sizeof s->cfg);
-  s->cfg.max_batch = 64;
+  s->cfg.max_batch = 128;
   if (cfg) s->cfg = *cfg;
-  if (s->cfg.max_batch <= 0) s->cfg.max_batch = 64;
+  if (s->cfg.max_batch <= 0) s->cfg.max_batch = 128;
   if (s->cfg.mode != 0 && s->cfg.mode != 1) {
     delete s;
     last_error() = "server mode must be 0 (batched) or 1 (plain)";

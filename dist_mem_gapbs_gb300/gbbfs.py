@@ -411,7 +411,7 @@ def msbfs_device(g, sources, depth_bytes=1):
     return ptr.value, st
 
 
-def msbfs_set_config(g, lanes=64, batch=8, alpha=15):
+def msbfs_set_config(g, lanes=128, batch=8, alpha=15):
     c = MsConfig(lanes, batch, alpha)
     _check(lib().gbbfs_msbfs_set_config(g.handle, ctypes.byref(c)), "msbfs_set_config")
 
@@ -471,7 +471,7 @@ class Server:
     PLAIN = 1
     BATCHED = 0
 
-    def __init__(self, mode=0, max_batch=64, hbm_budget_bytes=0, hbm_reserve_bytes=0):
+    def __init__(self, mode=0, max_batch=128, hbm_budget_bytes=0, hbm_reserve_bytes=0):
         cfg = ServerConfig(mode, max_batch, hbm_budget_bytes, hbm_reserve_bytes)
         h = ctypes.c_void_p()
         _check(lib().gbbfs_server_open(ctypes.byref(cfg), ctypes.byref(h)), "server_open")

@@ -219,7 +219,7 @@ typedef struct gbbfs_server gbbfs_server;
 
 typedef struct gbbfs_server_config {
   int32_t mode;              /* 0: batched multi-source; 1: one plain search per query */
-  int32_t max_batch;         /* queries per batch, <= lanes (default 64)         */
+  int32_t max_batch;         /* queries per batch, <= lanes (default 128)        */
   int64_t hbm_budget_bytes;  /* cap on per-graph search state, 0 = none          */
   int64_t hbm_reserve_bytes; /* free HBM to leave untouched                      */
 } gbbfs_server_config;
