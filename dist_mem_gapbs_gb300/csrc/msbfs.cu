@@ -472,6 +472,27 @@ bool same_cfg(const MsConfig& a, const MsConfig& b) {
   return a.lanes == b.lanes && a.batch == b.batch && a.alpha == b.alpha;
 }
 
+// Capture every (buffer, lane width) graph that is missing or was made for
+// another configuration, all at once: a first batch of a new width then
+// costs no capture (and its stream synchronize) in the middle of a run.
+int capture_all(gbbfs_graph* g) {
+  MsState* ms = g->ms;
+  bool synced = false;
+  for (int buf = 0; buf < 2; buf++)
+    for (int cls = 0; (32 << cls) <= ms->cfg.lanes; cls++) {
+      MsConfig want = ms->cfg;
+      want.lanes = 32 << cls;
+      if (ms->exec[buf][cls] && same_cfg(ms->exec_cfg[buf][cls], want)) continue;
+      if (!synced) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        synced = true;
+      }
+      GB_TRY(g->off32 ? capture_lanes<uint32_t>(g, buf, cls)
+                      : capture_lanes<unsigned long long>(g, buf, cls));
+    }
+  return GBBFS_OK;
+}
+
 // Launch one batch (k <= lanes sources) into depth buffer `buf`.
 int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
   MsState* ms = g->ms;
@@ -489,12 +510,7 @@ int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
   want.lanes = 32 << cls;
   // The buffer's previous results must have left the device first.
   GB_CUDA(cudaStreamWaitEvent(g->stream, ms->copied[buf], 0));
-  if (!ms->exec[buf][cls] || !same_cfg(ms->exec_cfg[buf][cls], want)) {
-    GB_CUDA(cudaStreamSynchronize(g->stream));
-    int rc = g->off32 ? capture_lanes<uint32_t>(g, buf, cls)
-                      : capture_lanes<unsigned long long>(g, buf, cls);
-    if (rc != GBBFS_OK) return rc;
-  }
+  if (!ms->exec[buf][cls] || !same_cfg(ms->exec_cfg[buf][cls], want)) GB_TRY(capture_all(g));
   // The host copy of the sources is read by the graph's first node; wait
   // until the previous launch that read this slot is done.
   GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
@@ -618,7 +634,8 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
 
 int ms_prepare(gbbfs_graph* g, int depth_bytes) {
   GB_CUDA(cudaSetDevice(g->device));
-  return ensure_state(g, depth_bytes);
+  GB_TRY(ensure_state(g, depth_bytes));
+  return capture_all(g);
 }
 
 int ms_lanes(const gbbfs_graph* g) { return g->ms ? g->ms->cfg.lanes : MsConfig().lanes; }
