@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "msbfs_kernels.cuh"
 
 namespace gbbfs {
 
@@ -98,8 +99,8 @@ struct Slot {
   gbbfs_graph* g = nullptr;
   std::deque<Query> pending;
   Inflight fl[2];
-  RowStats* d_stats = nullptr;   // 2 x 64
-  RowStats* h_stats = nullptr;   // pinned 2 x 64
+  RowStats* d_stats = nullptr;   // 2 x kMsMaxLanes (one block per batch buffer)
+  RowStats* h_stats = nullptr;   // pinned 2 x kMsMaxLanes
   uint8_t* d_plain = nullptr;    // plain mode: uint8 depth row
   bool admitted = false;
   double last_used = 0;
@@ -209,7 +210,7 @@ void harvest(gbbfs_server* s, Slot& sl) {
         if (cudaMemcpy(q.out, static_cast<uint8_t*>(ms_depth(sl.g, b)) + i * n, n,
                        cudaMemcpyDeviceToHost) != cudaSuccess)
           st = GBBFS_ERR_CUDA;
-      complete(s, sl, q, sl.h_stats[64 * b + i], st);
+      complete(s, sl, q, sl.h_stats[kMsMaxLanes * b + i], st);
     }
     f.q.clear();
     f.busy = false;
@@ -236,12 +237,14 @@ void launch(gbbfs_server* s, Slot& sl) {
     int st = ms_launch(sl.g, b, src.data(), k);
     if (st == GBBFS_OK) {
       cudaStream_t str = sl.g->stream;
-      cudaMemsetAsync(sl.d_stats + 64 * b, 0, sizeof(RowStats) * k, str);
+      cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str);
       const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
       k_row_stats<uint8_t><<<dim3(gx, k), 256, 0, str>>>(
-          static_cast<const uint8_t*>(ms_depth(sl.g, b)), sl.g->n, k, sl.d_stats + 64 * b,
+          static_cast<const uint8_t*>(ms_depth(sl.g, b)), sl.g->n, k,
+          sl.d_stats + kMsMaxLanes * b,
           nullptr);
-      cudaMemcpyAsync(sl.h_stats + 64 * b, sl.d_stats + 64 * b, sizeof(RowStats) * k,
+      cudaMemcpyAsync(sl.h_stats + kMsMaxLanes * b, sl.d_stats + kMsMaxLanes * b,
+                      sizeof(RowStats) * k,
                       cudaMemcpyDeviceToHost, str);
       ms_mark_copied(sl.g, b, str);
       cudaEventRecord(f.done, str);
@@ -370,8 +373,8 @@ int gbbfs_server_add_graph(gbbfs_server* s, gbbfs_graph* g, int32_t* graph_id) {
   }
   Slot sl;
   sl.g = g;
-  GB_CUDA(cudaMalloc(&sl.d_stats, sizeof(RowStats) * 128));
-  GB_CUDA(cudaHostAlloc(&sl.h_stats, sizeof(RowStats) * 128, cudaHostAllocDefault));
+  GB_CUDA(cudaMalloc(&sl.d_stats, sizeof(RowStats) * 2 * kMsMaxLanes));
+  GB_CUDA(cudaHostAlloc(&sl.h_stats, sizeof(RowStats) * 2 * kMsMaxLanes, cudaHostAllocDefault));
   GB_CUDA(cudaMalloc(&sl.d_plain, std::max<size_t>((size_t)g->n, 256)));
   for (int b = 0; b < 2; b++)
     GB_CUDA(cudaEventCreateWithFlags(&sl.fl[b].done, cudaEventDisableTiming));

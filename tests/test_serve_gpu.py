@@ -106,6 +106,22 @@ def test_admission_budget(native, pool):
             assert r["checksum"] == native.depth_checksum(exp[(r["graph_id"], r["source"])])
 
 
+def test_full_width_batches(native, pool):
+    """More queries on one graph than two batches of the widest lane word
+    hold: both batch buffers run full 128-query batches, every digest exact."""
+    off, g = pool[2]
+    srcs = [int(s) for s in native.pick_sources(off, 40)]
+    exp = {s: u8(native.DOBFS(g, s, depth=True)[1]) for s in srcs}
+    keys = [(0, srcs[i % len(srcs)]) for i in range(400)]
+    with native.Server(mode=0) as srv:
+        srv.add_graph(g)
+        res, _ = run_queries(native, srv, keys, [g.n], False)
+        assert max(r["batch_size"] for r in res) == 128
+        for r in res:
+            assert r["status"] == 0
+            assert r["checksum"] == native.depth_checksum(exp[r["source"]])
+
+
 def test_server_rejects(native, pool):
     with native.Server() as srv:
         gid = srv.add_graph(pool[0][1])
