@@ -464,12 +464,14 @@ def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=2048):
                     srv.submit(gid, sources[gid][0])
                 srv.drain()
                 srv.poll(4096)
-                # saturation: a burst of queries spread over the pool
+                # saturation: a burst of queries spread over the pool, handed
+                # to the server in one call
                 rng = np.random.default_rng(7)
+                gids = rng.integers(len(graphs), size=burst)
+                picks = rng.integers(256, size=burst)
+                srcs = [sources[int(gg)][int(pp)] for gg, pp in zip(gids, picks)]
                 t_start = srv.clock()
-                for _ in range(burst):
-                    gid = int(rng.integers(len(graphs)))
-                    srv.submit(gid, sources[gid][int(rng.integers(256))])
+                srv.submit_many(gids, srcs)
                 srv.drain()
                 res = srv.poll(burst + 16)
                 span = max(r["done_s"] for r in res) - t_start

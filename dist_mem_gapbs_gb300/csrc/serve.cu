@@ -411,6 +411,41 @@ int gbbfs_server_submit(gbbfs_server* s, int32_t graph_id, int32_t source, uint8
   return GBBFS_OK;
 }
 
+int gbbfs_server_submit_many(gbbfs_server* s, int64_t count, const int32_t* graph_ids,
+                             const int32_t* sources, uint8_t* const* depth_out,
+                             uint64_t* tickets) {
+  if (!s || count < 0 || (count > 0 && (!graph_ids || !sources))) return GBBFS_ERR_ARG;
+  for (int64_t i = 0; i < count; i++) {
+    if (graph_ids[i] < 0 || graph_ids[i] >= (int32_t)s->slots.size()) return GBBFS_ERR_ARG;
+    if (sources[i] < 0 || sources[i] >= s->slots[graph_ids[i]].g->n) {
+      last_error() = "source out of range";
+      return GBBFS_ERR_ARG;
+    }
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop) return GBBFS_ERR_STATE;
+  if (!s->started) {
+    s->started = true;
+    s->worker = std::thread(worker_loop, s);
+  }
+  const double t = s->now();
+  for (int64_t i = 0; i < count; i++) {
+    Query q;
+    q.ticket = s->next_ticket++;
+    q.graph = graph_ids[i];
+    q.source = sources[i];
+    q.out = depth_out ? depth_out[i] : nullptr;
+    q.t_submit = t;
+    q.t_start = q.t_done = 0;
+    q.batch = 0;
+    s->inbox.push_back(q);
+    s->outstanding++;
+    if (tickets) tickets[i] = q.ticket;
+  }
+  s->cv.notify_one();
+  return GBBFS_OK;
+}
+
 int gbbfs_server_poll(gbbfs_server* s, gbbfs_result* out, int32_t max, int32_t* count,
                       int32_t wait_us) {
   if (!s || !count || (max > 0 && !out)) return GBBFS_ERR_ARG;

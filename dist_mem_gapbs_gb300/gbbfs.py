@@ -35,7 +35,8 @@ EXPORTS = (
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
     "gbbfs_append_bfs_output", "gbbfs_msbfs", "gbbfs_msbfs_device", "gbbfs_msbfs_set_config",
     "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_msbfs_state_bytes", "gbbfs_server_open",
-    "gbbfs_server_add_graph", "gbbfs_server_submit", "gbbfs_server_poll", "gbbfs_server_drain",
+    "gbbfs_server_add_graph", "gbbfs_server_submit", "gbbfs_server_submit_many",
+    "gbbfs_server_poll", "gbbfs_server_drain",
     "gbbfs_server_clock", "gbbfs_server_close", "gbbfs_bfs_noalloc",
 )
 
@@ -138,6 +139,7 @@ def lib():
             "gbbfs_server_open": (I, [P, PP]),
             "gbbfs_server_add_graph": (I, [P, P, P]),
             "gbbfs_server_submit": (I, [P, i32, i32, P, P]),
+            "gbbfs_server_submit_many": (I, [P, i64, P, P, P, P]),
             "gbbfs_server_poll": (I, [P, P, i32, P, i32]),
             "gbbfs_server_drain": (I, [P, i32]),
             "gbbfs_server_clock": (ctypes.c_double, [P]),
@@ -492,6 +494,18 @@ class Server:
         if out is not None:
             self._keep[t.value] = out
         return t.value
+
+    def submit_many(self, graph_ids, sources):
+        """Queue a burst of (graph, source) queries at once (digests only);
+        returns their tickets."""
+        gids = np.ascontiguousarray(graph_ids, dtype=np.int32)
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        if gids.shape != src.shape:
+            raise ValueError("graph_ids and sources differ in length")
+        t = np.empty(len(src), np.uint64)
+        _check(lib().gbbfs_server_submit_many(self._h, len(src), _p(gids), _p(src), None,
+                                              _p(t)), "server_submit_many")
+        return [int(x) for x in t]
 
     def poll(self, max_results=1024, wait_us=0):
         buf = (Result * max_results)()

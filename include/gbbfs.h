@@ -244,6 +244,13 @@ int gbbfs_server_add_graph(gbbfs_server* s, gbbfs_graph* g, int32_t* graph_id);
 /* depth_out: host buffer of n bytes for the uint8 depth row, or NULL. */
 int gbbfs_server_submit(gbbfs_server* s, int32_t graph_id, int32_t source, uint8_t* depth_out,
                         uint64_t* ticket);
+/* count queries at once (a burst a front end received together): they are
+ * queued under one lock, so the batcher sees all of them before it fills
+ * lanes.  depth_out may be NULL, or hold count entries (each NULL or n
+ * bytes).  tickets (may be NULL) receives count tickets, in order. */
+int gbbfs_server_submit_many(gbbfs_server* s, int64_t count, const int32_t* graph_ids,
+                             const int32_t* sources, uint8_t* const* depth_out,
+                             uint64_t* tickets);
 /* Up to max finished results; waits up to wait_us for the first one. */
 int gbbfs_server_poll(gbbfs_server* s, gbbfs_result* out, int32_t max, int32_t* count,
                       int32_t wait_us);

@@ -122,6 +122,30 @@ def test_full_width_batches(native, pool):
             assert r["checksum"] == native.depth_checksum(exp[r["source"]])
 
 
+def test_submit_many(native, pool):
+    """A burst queued in one call: tickets in order, every digest exact."""
+    exp = expected(native, pool)
+    keys = list(exp) * 2
+    with native.Server(mode=0) as srv:
+        for _, g in pool:
+            srv.add_graph(g)
+        tickets = srv.submit_many([k[0] for k in keys], [k[1] for k in keys])
+        assert tickets == sorted(tickets) and len(set(tickets)) == len(keys)
+        srv.drain()
+        res = []
+        while True:
+            got = srv.poll(4096)
+            if not got:
+                break
+            res += got
+        assert len(res) == len(keys)
+        for r in res:
+            assert r["status"] == 0
+            assert r["checksum"] == native.depth_checksum(exp[(r["graph_id"], r["source"])])
+        with pytest.raises(native.GbbfsError):
+            srv.submit_many([0, 9], [1, 1])
+
+
 def test_server_rejects(native, pool):
     with native.Server() as srv:
         gid = srv.add_graph(pool[0][1])
