@@ -149,7 +149,7 @@ int upload(gbbfs_graph* g, const int64_t* offsets, const int32_t* neigh) {
   int64_t* tmp = nullptr;
   GB_CUDA(cudaMalloc(&tmp, sizeof(int64_t) * (g->n + 1)));
   cudaError_t e = cudaMemcpyAsync(tmp, offsets, sizeof(int64_t) * (g->n + 1),
-                                  cudaMemcpyHostToDevice, g->stream);
+                                  cudaMemcpyDefault, g->stream);
   if (e == cudaSuccess) {
     k_narrow_offsets<OffT><<<g->sms * 8, kThreads, 0, g->stream>>>(
         tmp, reinterpret_cast<OffT*>(g->off), g->n + 1);
@@ -162,7 +162,7 @@ int upload(gbbfs_graph* g, const int64_t* offsets, const int32_t* neigh) {
     return GBBFS_ERR_CUDA;
   }
   if (g->m > 0)
-    GB_CUDA(cudaMemcpyAsync(g->nbr, neigh, sizeof(int32_t) * g->m, cudaMemcpyHostToDevice,
+    GB_CUDA(cudaMemcpyAsync(g->nbr, neigh, sizeof(int32_t) * g->m, cudaMemcpyDefault,
                             g->stream));
   k_iso_mask<OffT><<<g->sms * 8, kThreads, 0, g->stream>>>(
       g->n, g->W, reinterpret_cast<const OffT*>(g->off), g->iso);
@@ -462,6 +462,25 @@ int search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
 }
 
 }  // namespace
+
+namespace gbbfs {
+
+// A handle from a CSR already in device memory (offsets int64[n+1],
+// neighbours int32[m]); the arrays are copied, the caller keeps them.
+int graph_create_device(const int64_t* d_off, const int32_t* d_nbr, int64_t n, int64_t m,
+                        gbbfs_graph** out) {
+  gbbfs_graph* g = new (std::nothrow) gbbfs_graph();
+  if (!g) return GBBFS_ERR_NOMEM;
+  const int rc = create(d_off, d_nbr, n, m, g);
+  if (rc != GBBFS_OK) {
+    release(g);
+    return rc;
+  }
+  *out = g;
+  return GBBFS_OK;
+}
+
+}  // namespace gbbfs
 
 extern "C" {
 

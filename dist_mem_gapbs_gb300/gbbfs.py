@@ -28,7 +28,8 @@ STEP_NAME = {STEP_TD: "td", STEP_E: "e", STEP_BU: "bu", STEP_C: "c"}
 
 # Every symbol include/gbbfs.h declares (the tests check the library exports them).
 EXPORTS = (
-    "gbbfs_graph_create", "gbbfs_graph_destroy", "gbbfs_graph_info", "gbbfs_bfs",
+    "gbbfs_graph_create", "gbbfs_graph_create_from_edges", "gbbfs_graph_csr",
+    "gbbfs_graph_destroy", "gbbfs_graph_info", "gbbfs_bfs",
     "gbbfs_bfs_many",
     "gbbfs_bfs_device", "gbbfs_results", "gbbfs_result_device_ptrs", "gbbfs_strerror",
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
@@ -114,6 +115,8 @@ def lib():
         sig = {
             "gbbfs_graph_create": (I, [P, P, i64, i64, PP]),
             "gbbfs_graph_destroy": (I, [P]),
+            "gbbfs_graph_create_from_edges": (I, [P, i64, i64, PP]),
+            "gbbfs_graph_csr": (I, [P, P, P]),
             "gbbfs_graph_info": (I, [P, P, P, P]),
             "gbbfs_bfs": (I, [P, i32, I, I, P, P, P]),
             "gbbfs_bfs_many": (I, [P, P, i64, I, I, P, P]),
@@ -200,6 +203,21 @@ def build_csr(edges, num_nodes=-1):
     return _take_csr(po, pn, n.value, m.value)
 
 
+def generate_edges(scale, degree=16, uniform=False):
+    """The generator's (E, 2) int32 edge list for -g/-u <scale> -k <degree>
+    (src/generator.h), before the CSR is built."""
+    L = lib()
+    pe, e = ctypes.c_void_p(), ctypes.c_int64()
+    _check(L.gbbfs_generate_edges(int(scale), int(degree), 1 if uniform else 0, ctypes.byref(pe),
+                                  ctypes.byref(e)), "generate_edges")
+    try:
+        arr = np.ctypeslib.as_array(ctypes.cast(pe, ctypes.POINTER(ctypes.c_int32)),
+                                    shape=(max(e.value, 1) * 2,))[:2 * e.value].copy()
+    finally:
+        L.gbbfs_free_host(pe)
+    return arr.reshape(-1, 2)
+
+
 def write_sg(path, offsets, neigh):
     off = np.ascontiguousarray(offsets, dtype=np.int64)
     nbr = np.ascontiguousarray(neigh, dtype=np.int32)
@@ -245,6 +263,33 @@ class Graph:
         _check(L.gbbfs_graph_create(_p(self._off), _p(nbr) if self.m else None, self.n, self.m,
                                     ctypes.byref(h)), "graph_create")
         self._h = h
+
+    @classmethod
+    def from_edges(cls, edges, num_nodes=-1):
+        """The graph of an (E, 2) int32 edge list, its CSR built on the GPU
+        (gbbfs_graph_create_from_edges)."""
+        L = lib()
+        el = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+        h = ctypes.c_void_p()
+        _check(L.gbbfs_graph_create_from_edges(_p(el) if len(el) else None, len(el),
+                                               int(num_nodes), ctypes.byref(h)),
+               "graph_create_from_edges")
+        self = cls.__new__(cls)
+        self._h = h
+        n, m = ctypes.c_int64(), ctypes.c_int64()
+        _check(L.gbbfs_graph_info(h, ctypes.byref(n), ctypes.byref(m), None), "graph_info")
+        self.n, self.m = n.value, m.value
+        self._off = np.empty(self.n + 1, np.int64)
+        _check(L.gbbfs_graph_csr(h, _p(self._off), None), "graph_csr")
+        return self
+
+    def csr(self):
+        """The handle's CSR copied back: (offsets int64[n+1], neigh int32[m])."""
+        off = np.empty(self.n + 1, np.int64)
+        nbr = np.empty(self.m, np.int32)
+        _check(lib().gbbfs_graph_csr(self.handle, _p(off), _p(nbr) if self.m else None),
+               "graph_csr")
+        return off, nbr
 
     @property
     def handle(self):

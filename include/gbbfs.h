@@ -82,6 +82,19 @@ typedef struct gbbfs_graph gbbfs_graph;
 int gbbfs_graph_create(const int64_t* offsets, const int32_t* neigh, int64_t n,
                        int64_t m_dir, gbbfs_graph** out);
 
+/* Builder::MakeGraph's CSR construction on the GPU (gapbs-verify/builder.h:
+ * 73-206: count degrees, prefix sum, scatter both directions, per-row sort,
+ * de-duplicate, drop self-loops): el_pairs holds `edges` (u, v) int32 pairs in
+ * host or device memory, num_nodes < 0 takes the largest id + 1.  The CSR is
+ * built in HBM (a radix sort of the directed edges) and becomes the handle's
+ * graph; it equals gbbfs_build_csr's byte for byte.  No host CSR is made. */
+int gbbfs_graph_create_from_edges(const int32_t* el_pairs, int64_t edges, int64_t num_nodes,
+                                  gbbfs_graph** out);
+
+/* Copy a handle's CSR to host memory: offsets int64[n+1] and neighbours
+ * int32[m_dir] (either may be NULL). */
+int gbbfs_graph_csr(const gbbfs_graph* g, int64_t* offsets_out, int32_t* neigh_out);
+
 /* Free the device copy (the graph's destructor, src/graph.h). */
 int gbbfs_graph_destroy(gbbfs_graph* g);
 
