@@ -256,13 +256,18 @@ def run_gbbfs(args):
     _build.build()
     scale, degree, uniform = GRAPHS[args.graph]
     t0 = time.time()
-    off, nbr = gbbfs.make_graph(scale, degree, uniform)
+    # The reference's generator on the host, the CSR built in HBM
+    # (gbbfs_graph_create_from_edges), the host copy read back for the CPU arm.
+    el = gbbfs.generate_edges(scale, degree, uniform)
+    gen_s = time.time() - t0
+    g = gbbfs.Graph.from_edges(el)
+    del el
+    off, nbr = g.csr()
     build_s = time.time() - t0
     n, m = len(off) - 1, len(nbr)
     all_sources = gbbfs.pick_sources(off, args.sources * world)
     sources = [int(s) for s in replica_sources(all_sources, rank, world, args.sources)]
     deg = np.diff(off)
-    g = gbbfs.Graph(off, nbr)
 
     # Untimed instrumented pass: per-source reached edges and per-step byte counts.
     info = {}
@@ -376,7 +381,7 @@ def run_gbbfs(args):
                     "d2h_bytes_per_step": 4 * n * len(sources)},
             "gpu_launches": launches,
             "clocks": clocks.summary(),
-            "device_busy_s": busy, "graph_build_s": build_s,
+            "device_busy_s": busy, "graph_build_s": build_s, "graph_generate_s": gen_s,
         }
     g.close()
     del off, nbr
@@ -397,8 +402,8 @@ def run_gbbfs(args):
 def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
     """Batched multi-source BFS on Kronecker-24: queries/s for 4096 sources
     against back-to-back plain single-source launches, rows spot-checked."""
-    off, nbr = gbbfs.make_graph(scale, 16, False)
-    with gbbfs.Graph(off, nbr) as g:
+    with gbbfs.Graph.from_edges(gbbfs.generate_edges(scale, 16, False)) as g:
+        off = g.offsets
         srcs = gbbfs.pick_sources(off, queries)
         for s in srcs[:8]:
             gbbfs.bfs_device(g, int(s))
@@ -448,10 +453,9 @@ def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=2048):
     graphs, sources = [], []
     t0 = time.time()
     for sc, uni in pool:
-        off, nbr = gbbfs.make_graph(sc, 16, uni)
-        graphs.append(gbbfs.Graph(off, nbr))
-        sources.append([int(s) for s in gbbfs.pick_sources(off, 256)])
-        del off, nbr
+        g = gbbfs.Graph.from_edges(gbbfs.generate_edges(sc, 16, uni))
+        graphs.append(g)
+        sources.append([int(s) for s in gbbfs.pick_sources(g.offsets, 256)])
     build_s = time.time() - t0
     out = {"pool": ["%s%d" % ("u" if u else "g", s) for s, u in pool], "build_s": build_s}
     try:

@@ -137,14 +137,29 @@ int main(int argc, char** argv) {
 
   int64_t *off = nullptr, n = 0, m = 0;
   int32_t* nbr = nullptr;
+  gbbfs_graph* g = nullptr;
   int rc;
   if (o.scale != -1) {
-    rc = gbbfs_generate(o.scale, o.degree, o.uniform ? 1 : 0, &off, &nbr, &n, &m);
+    // Generated graphs: the edge list from the host generator, the CSR built
+    // in HBM; the host keeps the offsets (and the neighbours for --sg-out).
+    int32_t* el = nullptr;
+    int64_t edges = 0;
+    rc = gbbfs_generate_edges(o.scale, o.degree, o.uniform ? 1 : 0, &el, &edges);
+    if (rc == GBBFS_OK) rc = gbbfs_graph_create_from_edges(el, edges, -1, &g);
+    gbbfs_free_host(el);
+    if (rc == GBBFS_OK) rc = gbbfs_graph_info(g, &n, &m, nullptr);
+    if (rc == GBBFS_OK) {
+      off = static_cast<int64_t*>(malloc(sizeof(int64_t) * (n + 1)));
+      if (!o.sg_out.empty()) nbr = static_cast<int32_t*>(malloc(sizeof(int32_t) * (m + 1)));
+      rc = !off || (!o.sg_out.empty() && !nbr) ? GBBFS_ERR_NOMEM
+                                               : gbbfs_graph_csr(g, off, nbr);
+    }
   } else {
     rc = gbbfs_read_graph(o.filename.c_str(), o.symmetrize ? 1 : 0, &off, &nbr, &n, &m);
   }
   if (rc != GBBFS_OK) {
-    fprintf(stderr, "graph construction failed: %s\n", gbbfs_strerror(rc));
+    fprintf(stderr, "graph construction failed: %s (%s)\n", gbbfs_strerror(rc),
+            gbbfs_last_error());
     return 1;
   }
   if (!o.sg_out.empty()) {
@@ -160,8 +175,7 @@ int main(int argc, char** argv) {
          "\n",
          prefix(), n, undirected, undirected / n);
 
-  gbbfs_graph* g = nullptr;
-  rc = gbbfs_graph_create(off, nbr, n, m, &g);
+  if (!g) rc = gbbfs_graph_create(off, nbr, n, m, &g);
   if (rc != GBBFS_OK) {
     fprintf(stderr, "gbbfs_graph_create: %s (%s)\n", gbbfs_strerror(rc), gbbfs_last_error());
     return 1;

@@ -297,6 +297,11 @@ class Graph:
             raise GbbfsError(ERR_STATE, "graph closed")
         return self._h
 
+    @property
+    def offsets(self):
+        """The CSR offsets (host copy, int64[n+1])."""
+        return self._off
+
     def num_nodes(self):
         return self.n
 
