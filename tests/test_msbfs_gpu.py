@@ -97,3 +97,10 @@ def test_msbfs_device_and_autotune(native):
         assert ptr and st.batches == 1
         with pytest.raises(native.GbbfsError):
             native.msbfs_device(g, srcs[:10].tolist() + [len(off) + 5], 1)
+
+
+def test_msbfs_cli(native, capsys):
+    from dist_mem_gapbs_gb300 import msbfs_cli
+    assert msbfs_cli.main(["-g", "12", "-n", "40", "--lanes", "32", "--levels"]) == 0
+    out = capsys.readouterr().out
+    assert out.count("batch ") == 2 and "queries/s" in out and "level  1" in out
