@@ -338,6 +338,52 @@ void orc_depth(const int64_t* off, const int32_t* nbr, int64_t n, int32_t source
   }
 }
 
+// BC's BFS phase, serial: PBFS of gapbs-verify/bc.cc:51-92 (src/bc.cc:55-102
+// in the DMM copy, whose path counts are unsigned long long and add with
+// wrap-around).  Level by level over the queue: an unvisited neighbour gets
+// the next depth and is queued; every edge into a vertex of the next depth
+// sets its successor bit (bit e of the edge bitmap) and adds the path count
+// of its tail.  level_start gets levels + 1 entries; returns levels.
+int32_t orc_bc_bfs(const int64_t* off, const int32_t* nbr, int64_t n, int32_t source,
+                   uint64_t* sigma, int32_t* depth, uint32_t* succ, int32_t* order,
+                   int64_t* level_start) {
+  const int64_t m = off[n];
+  for (int64_t v = 0; v < n; v++) {
+    depth[v] = -1;
+    sigma[v] = 0;
+  }
+  for (int64_t w = 0; w < (m + 31) / 32; w++) succ[w] = 0;
+  depth[source] = 0;
+  sigma[source] = 1;
+  int64_t qs = 0, qe = 1;
+  order[0] = source;
+  int32_t levels = 0;
+  level_start[0] = 0;
+  while (qs < qe) {
+    const int32_t d = levels + 1;
+    int64_t tail = qe;
+    for (int64_t i = qs; i < qe; i++) {
+      const int32_t u = order[i];
+      for (int64_t e = off[u]; e < off[u + 1]; e++) {
+        const int32_t v = nbr[e];
+        if (depth[v] == -1) {
+          depth[v] = d;
+          order[tail++] = v;
+        }
+        if (depth[v] == d) {
+          succ[e >> 5] |= 1u << (e & 31);
+          sigma[v] += sigma[u];
+        }
+      }
+    }
+    levels++;
+    level_start[levels] = qe;
+    qs = qe;
+    qe = tail;
+  }
+  return levels;
+}
+
 // BFSVerifier: gapbs-verify/bfs.cc:195-241.  Returns 1 on PASS, 0 on FAIL;
 // *why gets 1 "source wrong", 2 "wrong depths", 3 "no such edge",
 // 4 "reachability mismatch".

@@ -47,6 +47,8 @@ def lib():
         L.orc_verify.argtypes = [P, P, i64, ctypes.c_int32, P, ctypes.POINTER(ctypes.c_int)]
         L.orc_alg_bytes.restype = i64
         L.orc_alg_bytes.argtypes = [i64, P, ctypes.c_int]
+        L.orc_bc_bfs.restype = ctypes.c_int32
+        L.orc_bc_bfs.argtypes = [P, P, i64, ctypes.c_int32, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -181,3 +183,21 @@ def parse_trace(stdout):
         elif runs and f[0] in ("e", "c"):
             runs[-1][1].append((f[0], 0))
     return runs
+
+
+def bc_bfs(off, nbr, source):
+    """BC's BFS phase (gapbs-verify/bc.cc:51-92), serial: (path counts
+    uint64[n], depth int32[n], successor bitmap uint32[(m+31)//32], order of
+    the reached vertices int32, level starts int64[levels + 1])."""
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    n = len(off) - 1
+    sigma = np.empty(n, np.uint64)
+    dep = np.empty(n, np.int32)
+    succ = np.empty(max(1, (len(nbr) + 31) // 32), np.uint32)
+    order = np.empty(max(n, 1), np.int32)
+    starts = np.empty(n + 2, np.int64)
+    levels = lib().orc_bc_bfs(_ptr(off), _ptr(nbr), n, int(source), _ptr(sigma), _ptr(dep),
+                              _ptr(succ), _ptr(order), _ptr(starts))
+    reached = int(starts[levels])
+    return sigma, dep, succ[:(len(nbr) + 31) // 32], order[:reached], starts[:levels + 1]
