@@ -31,7 +31,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function",
              "-I", INCLUDE, "-I", CSRC]
 
-CUDA_SOURCES = ["bfs_engine.cu", "msbfs.cu", "serve.cu", "noalloc.cu", "gpu_build.cu"]
+CUDA_SOURCES = ["bfs_engine.cu", "msbfs.cu", "serve.cu", "noalloc.cu", "gpu_build.cu", "bc.cu"]
 CXX_SOURCES = ["host_graph.cc", "host_io.cc"]
 
 

@@ -59,6 +59,8 @@ void release(gbbfs_graph* g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   msbfs_release(g->ms);
   g->ms = nullptr;
+  bc_release(g->bc);
+  g->bc = nullptr;
   if (g->copy_stream) cudaStreamSynchronize(g->copy_stream);
   for (int i = 0; i < 2; i++) {
     cudaFree(g->stage[i]);

@@ -21,6 +21,8 @@ inline std::string& last_error() {
 
 struct MsState;   // multi-source BFS buffers of a handle (msbfs.cu)
 void msbfs_release(MsState* ms);
+struct BcState;   // BC BFS-phase buffers of a handle (bc.cu)
+void bc_release(BcState* b);
 
 }  // namespace gbbfs
 
@@ -93,6 +95,7 @@ struct gbbfs_graph {
   bool have_result = false;
   bool result_depth = false;
   gbbfs::MsState* ms = nullptr;
+  gbbfs::BcState* bc = nullptr;
   // gbbfs_bfs_many: staged parent arrays and their copy-out stream.
   int32_t* stage[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;

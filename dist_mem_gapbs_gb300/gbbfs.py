@@ -30,7 +30,7 @@ STEP_NAME = {STEP_TD: "td", STEP_E: "e", STEP_BU: "bu", STEP_C: "c"}
 EXPORTS = (
     "gbbfs_graph_create", "gbbfs_graph_create_from_edges", "gbbfs_graph_csr",
     "gbbfs_graph_destroy", "gbbfs_graph_info", "gbbfs_bfs",
-    "gbbfs_bfs_many",
+    "gbbfs_bfs_many", "gbbfs_bc_bfs",
     "gbbfs_bfs_device", "gbbfs_results", "gbbfs_result_device_ptrs", "gbbfs_strerror",
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
@@ -120,6 +120,7 @@ def lib():
             "gbbfs_graph_info": (I, [P, P, P, P]),
             "gbbfs_bfs": (I, [P, i32, I, I, P, P, P]),
             "gbbfs_bfs_many": (I, [P, P, i64, I, I, P, P]),
+            "gbbfs_bc_bfs": (I, [P, i32, P, P, P, P, P, P]),
             "gbbfs_bfs_device": (I, [P, i32, I, I, I, P]),
             "gbbfs_results": (I, [P, P, P]),
             "gbbfs_result_device_ptrs": (I, [P, PP, PP]),
@@ -415,6 +416,23 @@ def bfs_many(g, sources, out, alpha=15, beta=18):
     _check(lib().gbbfs_bfs_many(g.handle, _p(src), k, int(alpha), int(beta), ptrs, None),
            "bfs_many")
     return out
+
+
+def bc_bfs(g, source):
+    """BC's BFS phase (src/bc.cc:55-102): (path counts uint64[n], depth
+    int32[n], successor bitmap uint32[(m+31)//32], reached vertices in level
+    order int32, level starts int64[levels + 1])."""
+    n, m = g.n, g.m
+    sigma = np.empty(n, np.uint64)
+    dep = np.empty(n, np.int32)
+    succ = np.empty(max(1, (m + 31) // 32), np.uint32)
+    order = np.empty(max(n, 1), np.int32)
+    starts = np.empty(n + 1, np.int64)
+    levels = ctypes.c_int32()
+    _check(lib().gbbfs_bc_bfs(g.handle, int(source), _p(sigma), _p(dep), _p(succ), _p(order),
+                              _p(starts), ctypes.byref(levels)), "bc_bfs")
+    lv = levels.value
+    return sigma, dep, succ[:(m + 31) // 32], order[:int(starts[lv])], starts[:lv + 1]
 
 
 def bfs_device(g, source, alpha=15, beta=18, want_depth=False, stats=False, instrument=False,

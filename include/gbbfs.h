@@ -156,6 +156,23 @@ int gbbfs_results(gbbfs_graph* g, int32_t* parent_out, int32_t* depth_out);
 int gbbfs_result_device_ptrs(gbbfs_graph* g, const int32_t** parent,
                              const int32_t** depth);
 
+/* BC's BFS phase from `source` (src/bc.cc:55-102; gapbs-verify/bc.cc:51-92):
+ * a level-synchronous BFS over every edge of each level.  Host outputs, each
+ * may be NULL:
+ *   path_counts uint64[n]  shortest paths from the source (the reference's
+ *                          unsigned long long adds, so modulo 2^64); 0 when
+ *                          unreached
+ *   depth       int32[n]   -1 when unreached
+ *   succ        uint32[(m_dir+31)/32]  bit e%32 of word e/32 set when the
+ *                          directed edge at CSR position e leads one level
+ *                          down (the successor bitmap)
+ *   order       int32[n]   the reached vertices level by level (the order
+ *                          inside a level is not specified)
+ *   level_start int64[n+1] level d is order[level_start[d] .. level_start[d+1])
+ * *levels (may be NULL) receives the number of levels, the source's being 0. */
+int gbbfs_bc_bfs(gbbfs_graph* g, int32_t source, uint64_t* path_counts, int32_t* depth,
+                 uint32_t* succ, int32_t* order, int64_t* level_start, int32_t* levels);
+
 /* ---- Batched multi-source BFS (no reference counterpart) ----
  * Many sources of one graph at once, 32, 64 or 128 per batch as a bitmask per
  * vertex, in one persistent kernel per batch captured in a CUDA graph.  Its
