@@ -383,9 +383,17 @@ def run_gbbfs(args):
             "clocks": clocks.summary(),
             "device_busy_s": busy, "graph_build_s": build_s, "graph_generate_s": gen_s,
         }
+    bc_line = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        try:
+            bc_line = run_bc(gbbfs, g, sources[:5], deg)
+        except Exception as exc:  # reported, never hides the main line
+            bc_line = {"error": "%s: %s" % (type(exc).__name__, exc)}
     g.close()
     del off, nbr
     if rank == 0:
+        if bc_line is not None:
+            line["bc_bfs_phase"] = bc_line
         if world == 1 and not args.no_extras:
             # The metric's other two parts: batched queries/s and served p50/p99.
             for key, fn in (("batched", run_batched), ("serving", run_serving)):
@@ -397,6 +405,23 @@ def run_gbbfs(args):
     if tdist is not None:
         tdist.destroy_process_group()
     return 0
+
+
+def run_bc(gbbfs, g, sources, deg):
+    """BC's BFS phase (gbbfs_bc_bfs) on the metric's graph: wall time per
+    source with the path counts, depths, successor bitmap and level order
+    copied to host memory."""
+    gbbfs.bc_bfs(g, sources[0])                            # state allocated
+    ms, rate = [], []
+    for s in sources[1:]:
+        t = time.perf_counter()
+        _, _, _, order, starts = gbbfs.bc_bfs(g, s)
+        dt = time.perf_counter() - t
+        ms.append(dt * 1e3)
+        rate.append(float(deg[order].sum()) / dt / 1e9)
+    return {"sources": len(ms), "ms_per_source": float(np.mean(ms)),
+            "edges_per_s_g": float(np.mean(rate)), "levels": int(len(starts) - 1),
+            "includes": "device->host copies of all four results"}
 
 
 def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
