@@ -1,8 +1,9 @@
 // Graph file input/output for the host side of the BFS path.
 //
 // Formats follow the reference's Reader / Writer: ".sg" serialized graphs
-// (src/writer.h:39-69, src/reader.h:291-345), ".el" and ".wel" edge lists and
-// DIMACS ".gr" files (gapbs-verify/reader.h:49-84).  Edge lists go through
+// (src/writer.h:39-69, src/reader.h:291-345), ".el" and ".wel" edge lists,
+// DIMACS ".gr" files (gapbs-verify/reader.h:49-84) and Matrix Market ".mtx"
+// coordinate files (src/reader.h:186-256).  Edge lists go through
 // gbbfs_build_csr, the same construction the synthetic graphs use.
 
 #include <cstdint>
@@ -72,6 +73,77 @@ int ReadEdgeText(const std::string& path, bool dimacs, int per_edge,
   return rc;
 }
 
+// Matrix Market coordinate files (src/reader.h:186-256): a header line
+// "%%MatrixMarket matrix coordinate <field> <symmetry>", '%' comment lines,
+// "rows cols entries" (square only), then one 1-based "row col [value]" entry
+// per line.  Fields pattern / real / double / integer (values are ignored),
+// symmetries symmetric (undirected) / general / skew-symmetric.
+int ReadMTX(const std::string& path, std::vector<int32_t>* el, bool* undirected) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return GBBFS_ERR_IO;
+  char start[64] = {0}, object[64] = {0}, format[64] = {0}, field[64] = {0}, sym[64] = {0};
+  int rc = GBBFS_OK;
+  if (fscanf(f, "%63s %63s %63s %63s %63s", start, object, format, field, sym) != 5 ||
+      strcmp(start, "%%MatrixMarket") != 0 || strcmp(object, "matrix") != 0 ||
+      strcmp(format, "coordinate") != 0)
+    rc = GBBFS_ERR_IO;
+  bool weighted = false;
+  if (rc == GBBFS_OK) {
+    if (strcmp(field, "pattern") == 0)
+      weighted = false;
+    else if (!strcmp(field, "real") || !strcmp(field, "double") || !strcmp(field, "integer"))
+      weighted = true;
+    else
+      rc = GBBFS_ERR_IO;   // complex or unknown
+    if (strcmp(sym, "symmetric") == 0)
+      *undirected = true;
+    else if (!strcmp(sym, "general") || !strcmp(sym, "skew-symmetric"))
+      *undirected = false;
+    else
+      rc = GBBFS_ERR_IO;
+  }
+  char* lp = nullptr;
+  size_t cap = 0;
+  bool sized = false;
+  while (rc == GBBFS_OK && getline(&lp, &cap, f) >= 0) {
+    const char* p = lp;
+    while (*p == ' ' || *p == '\t') p++;
+    if (*p == '%' || *p == '\n' || *p == '\r' || *p == '\0') continue;
+    long long a = 0, b = 0, c = 0;
+    char* end = nullptr;
+    a = strtoll(p, &end, 10);
+    if (end == p) {
+      rc = GBBFS_ERR_IO;
+      break;
+    }
+    p = end;
+    b = strtoll(p, &end, 10);
+    if (end == p) {
+      rc = GBBFS_ERR_IO;
+      break;
+    }
+    p = end;
+    if (!sized) {
+      c = strtoll(p, &end, 10);
+      if (end == p || a != b) rc = GBBFS_ERR_IO;   // entries count; square only
+      sized = true;
+      continue;
+    }
+    (void)weighted;   // a value, if present, is ignored
+    const long long u = a - 1, v = b - 1;
+    if (u < 0 || v < 0 || u > INT32_MAX || v > INT32_MAX) {
+      rc = GBBFS_ERR_IO;
+      break;
+    }
+    el->push_back(static_cast<int32_t>(u));
+    el->push_back(static_cast<int32_t>(v));
+  }
+  if (rc == GBBFS_OK && !sized) rc = GBBFS_ERR_IO;
+  free(lp);
+  fclose(f);
+  return rc;
+}
+
 int ReadSG(const std::string& path, int64_t** offsets_out, int32_t** neigh_out,
            int64_t* n_out, int64_t* m_out) {
   FILE* f = fopen(path.c_str(), "rb");
@@ -124,6 +196,7 @@ int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
   const std::string p(path), suf = Suffix(p);
   if (suf == ".sg") return ReadSG(p, offsets_out, neigh_out, n_out, m_dir_out);
   std::vector<int32_t> el;
+  bool undirected = false;
   int rc;
   if (suf == ".el")
     rc = ReadEdgeText(p, false, 2, &el);
@@ -131,10 +204,13 @@ int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
     rc = ReadEdgeText(p, false, 3, &el);
   else if (suf == ".gr")
     rc = ReadEdgeText(p, true, 3, &el);
+  else if (suf == ".mtx")
+    rc = ReadMTX(p, &el, &undirected);
   else
     return GBBFS_ERR_ARG;
   if (rc != GBBFS_OK) return rc;
-  if (!symmetrize) return GBBFS_ERR_ARG;  // directed graphs are outside this engine
+  // directed graphs are outside this engine; a symmetric .mtx is undirected
+  if (!symmetrize && !undirected) return GBBFS_ERR_ARG;
   if (el.empty()) return GBBFS_ERR_IO;
   return gbbfs_build_csr(el.data(), static_cast<int64_t>(el.size() / 2), -1, offsets_out,
                          neigh_out, n_out, m_dir_out);

@@ -121,6 +121,34 @@ def test_edge_list_files(native, tmp_path):
         native.make_graph(filename=str(el), symmetrize=False)
 
 
+def test_matrix_market_files(native, tmp_path):
+    rng = np.random.default_rng(2)
+    edges = rng.integers(0, 50, size=(300, 2))
+    ro, rn = _reference_csr(edges)
+    body = "".join("%d %d\n" % (u + 1, v + 1) for u, v in edges)
+    gen = tmp_path / "g.mtx"
+    gen.write_text("%%MatrixMarket matrix coordinate pattern general\n% a comment\n"
+                   "50 50 300\n" + body)
+    off, nbr = native.make_graph(filename=str(gen), symmetrize=True)
+    assert np.array_equal(off[:len(ro)], ro) and np.array_equal(nbr, rn)
+    with pytest.raises(native.GbbfsError):   # general = directed: needs -s
+        native.make_graph(filename=str(gen), symmetrize=False)
+    # a symmetric file lists each edge once; weights are ignored
+    sym = tmp_path / "s.mtx"
+    sym.write_text("%%MatrixMarket matrix coordinate real symmetric\n50 50 300\n" +
+                   "".join("%d %d 0.5\n" % (u + 1, v + 1) for u, v in edges))
+    o2, n2 = native.make_graph(filename=str(sym), symmetrize=False)
+    assert np.array_equal(o2, off) and np.array_equal(n2, nbr)
+    for bad in ("%%MatrixMarket matrix coordinate complex general\n50 50 1\n1 2 1 1\n",
+                "%%MatrixMarket matrix array real general\n50 50 1\n1 2 1\n",
+                "%%MatrixMarket matrix coordinate pattern general\n50 40 1\n1 2\n",
+                "not a header\n"):
+        f = tmp_path / "bad.mtx"
+        f.write_text(bad)
+        with pytest.raises(native.GbbfsError):
+            native.make_graph(filename=str(f), symmetrize=True)
+
+
 def test_bfs_output_writer(native, tmp_path):
     p = str(tmp_path / "bfs_output.txt")
     a = np.array([3, -1, -7, 0, 2147483647, -2147483648], np.int32)
