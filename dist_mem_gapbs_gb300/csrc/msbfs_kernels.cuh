@@ -559,9 +559,12 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
     }
 
     if (!bottom_up) {
-      // A frontier with many edges reaches many vertices: install the next
-      // frontier by one pass over all vertices instead of a touched list.
-      const bool dense = E > (unsigned long long)(a.n >> 4);
+      // A frontier with many edges, early in the search, reaches many new
+      // vertices: install the next frontier by one pass over all vertices
+      // instead of a touched list.  After a bottom-up level (or a dense
+      // install) most targets are visited already, so the list is small
+      // unless the frontier's degree sum exceeds n.
+      const bool dense = E > (unsigned long long)(have_queue ? a.n >> 4 : a.n);
       if (!have_queue) {
         // The frontier was written densely (bottom-up or dense install):
         // queue it from its fbits.  (q_packed[cur] was reset a level ago.)
