@@ -1,4 +1,6 @@
-// BC's BFS phase on the GPU (src/bc.cc:55-102; gapbs-verify/bc.cc:51-92).
+// Betweenness centrality on the GPU: BC's BFS phase (src/bc.cc:55-102;
+// gapbs-verify/bc.cc:51-92) and, for gbbfs_bc, Brandes' back-propagation and
+// normalization (src/bc.cc:106-171).
 //
 // Brandes' betweenness centrality first runs, from each source, a
 // level-synchronous BFS that records for every vertex its depth and its
@@ -19,6 +21,12 @@
 // u's count is final: all of its in-edges lie in the level before.  Results
 // equal the serial restatement exactly; only the order of vertices inside a
 // level depends on timing, as in the reference.
+//
+// Back-propagation walks the levels from the deepest up, a warp per vertex:
+// a vertex's dependency sums path_counts[u] / path_counts[v] * (1 + delta[v])
+// over its successor edges (terms in double, as the DMM code computes them,
+// summed in a fixed order), and is added to its score.  Scores are divided by
+// their maximum at the end.
 
 #include <cuda_runtime.h>
 
@@ -33,6 +41,8 @@ namespace gbbfs {
 
 struct BcState {
   int64_t n = 0, m = 0;
+  float* delta = nullptr;    // dependency of the current source (Brandes)
+  float* score = nullptr;    // scores summed over the sources
   unsigned long long* sigma = nullptr;
   int32_t* depth = nullptr;
   uint32_t* succ = nullptr;
@@ -51,6 +61,8 @@ void bc_release(BcState* b) {
   cudaFree(b->degs);
   cudaFree(b->epre);
   cudaFree(b->tail);
+  cudaFree(b->delta);
+  cudaFree(b->score);
   delete b;
 }
 
@@ -157,6 +169,57 @@ __global__ void __launch_bounds__(kThreads) k_bc_expand(
   }
 }
 
+// Dependencies of one level (src/bc.cc:129-152, gapbs-verify/bc.cc:128-141):
+// for u in the level, delta[u] = sum over u's successor edges (u, v) of
+// path_counts[u] / path_counts[v] * (1 + delta[v]), added to u's score.  A
+// warp per vertex; terms in double, summed in a fixed lane order.
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_bc_back(const OffT* off, const int32_t* nbr,
+                                                      const uint32_t* succ,
+                                                      const unsigned long long* sigma,
+                                                      const int32_t* level, int64_t count,
+                                                      float* delta, float* score) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < count; i += nwarps) {
+    const int32_t u = level[i];
+    const uint64_t b = (uint64_t)off[u], e = (uint64_t)off[u + 1];
+    const double su = (double)sigma[u];
+    double sum = 0.0;
+    for (uint64_t j = b + lane; j < e; j += 32) {
+      if ((__ldg(succ + (j >> 5)) >> (j & 31)) & 1u) {
+        const int32_t v = nbr[j];
+        sum += su / (double)sigma[v] * (1.0 + (double)delta[v]);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+    if (lane == 0) {
+      delta[u] = (float)sum;
+      score[u] += (float)sum;
+    }
+  }
+}
+
+__global__ void k_max_f(const float* x, int64_t n, unsigned int* out_bits) {
+  float mx = 0.0f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    mx = fmaxf(mx, x[i]);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+  // scores are >= 0, so their bit patterns order like the values
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(mx));
+}
+
+__global__ void k_scale_f(float* x, int64_t n, const unsigned int* max_bits) {
+  const float mx = __uint_as_float(*max_bits);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = x[i] / mx;
+}
+
 int ensure_bc(gbbfs_graph* g) {
   if (g->bc) return GBBFS_OK;
   BcState* b = new BcState();
@@ -171,13 +234,15 @@ int ensure_bc(gbbfs_graph* g) {
   if (e == cudaSuccess) e = cudaMalloc(&b->degs, 4 * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b->epre, 8 * (n + 2));
   if (e == cudaSuccess) e = cudaMalloc(&b->tail, 8);
+  if (e == cudaSuccess) e = cudaMalloc(&b->delta, 4 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->score, 4 * n);
   if (e != cudaSuccess) {
     bc_release(b);
     last_error() = std::string("BC state: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? GBBFS_ERR_NOMEM : GBBFS_ERR_CUDA;
   }
   g->bc = b;
-  g->device_bytes += (int64_t)(8 * n + 4 * n + 4 * words + 8 * (n + 1) + 8 * (n + 2) + 8);
+  g->device_bytes += (int64_t)(8 * n + 4 * n + 4 * words + 8 * (n + 1) + 8 * (n + 2) + 8 + 8 * n);
   return GBBFS_OK;
 }
 
@@ -225,10 +290,55 @@ int run_bc(gbbfs_graph* g, int32_t source, std::vector<int64_t>* starts) {
   return GBBFS_OK;
 }
 
+template <typename OffT>
+int run_brandes(gbbfs_graph* g, const int32_t* sources, int64_t k) {
+  BcState* b = g->bc;
+  cudaStream_t s = g->stream;
+  const OffT* off = reinterpret_cast<const OffT*>(g->off);
+  GB_CUDA(cudaMemsetAsync(b->score, 0, 4 * (size_t)g->n, s));
+  std::vector<int64_t> starts;
+  for (int64_t i = 0; i < k; i++) {
+    GB_TRY(run_bc<OffT>(g, sources[i], &starts));
+    GB_CUDA(cudaMemsetAsync(b->delta, 0, 4 * (size_t)g->n, s));
+    for (int64_t d = (int64_t)starts.size() - 2; d >= 0; d--) {
+      const int64_t count = starts[d + 1] - starts[d];
+      k_bc_back<OffT><<<g->sms * 8, kThreads, 0, s>>>(off, g->nbr, b->succ, b->sigma,
+                                                       b->queue + starts[d], count, b->delta,
+                                                       b->score);
+      GB_CUDA(cudaGetLastError());
+    }
+  }
+  // scores / their maximum (src/bc.cc:160-167)
+  GB_CUDA(cudaMemsetAsync(b->tail, 0, 8, s));
+  unsigned int* mx = reinterpret_cast<unsigned int*>(b->tail);
+  k_max_f<<<g->sms * 8, kThreads, 0, s>>>(b->score, g->n, mx);
+  k_scale_f<<<g->sms * 8, kThreads, 0, s>>>(b->score, g->n, mx);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(s));
+  return GBBFS_OK;
+}
+
 }  // namespace
 }  // namespace gbbfs
 
 extern "C" {
+
+int gbbfs_bc(gbbfs_graph* g, const int32_t* sources, int64_t k, float* scores_out) {
+  if (!g || k < 1 || !sources) return GBBFS_ERR_ARG;
+  for (int64_t i = 0; i < k; i++)
+    if (sources[i] < 0 || sources[i] >= g->n) {
+      gbbfs::last_error() = "source out of range";
+      return GBBFS_ERR_ARG;
+    }
+  GB_CUDA(cudaSetDevice(g->device));
+  GB_TRY(gbbfs::ensure_bc(g));
+  GB_TRY(g->off32 ? gbbfs::run_brandes<uint32_t>(g, sources, k)
+                  : gbbfs::run_brandes<unsigned long long>(g, sources, k));
+  if (scores_out)
+    GB_CUDA(cudaMemcpy(scores_out, g->bc->score, 4 * (size_t)g->n, cudaMemcpyDeviceToHost));
+  return GBBFS_OK;
+}
+
 
 int gbbfs_bc_bfs(gbbfs_graph* g, int32_t source, uint64_t* path_counts, int32_t* depth,
                  uint32_t* succ, int32_t* order, int64_t* level_start, int32_t* levels) {

@@ -30,7 +30,7 @@ STEP_NAME = {STEP_TD: "td", STEP_E: "e", STEP_BU: "bu", STEP_C: "c"}
 EXPORTS = (
     "gbbfs_graph_create", "gbbfs_graph_create_from_edges", "gbbfs_graph_csr",
     "gbbfs_graph_destroy", "gbbfs_graph_info", "gbbfs_bfs",
-    "gbbfs_bfs_many", "gbbfs_bc_bfs",
+    "gbbfs_bfs_many", "gbbfs_bc_bfs", "gbbfs_bc",
     "gbbfs_bfs_device", "gbbfs_results", "gbbfs_result_device_ptrs", "gbbfs_strerror",
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
@@ -121,6 +121,7 @@ def lib():
             "gbbfs_bfs": (I, [P, i32, I, I, P, P, P]),
             "gbbfs_bfs_many": (I, [P, P, i64, I, I, P, P]),
             "gbbfs_bc_bfs": (I, [P, i32, P, P, P, P, P, P]),
+            "gbbfs_bc": (I, [P, P, i64, P]),
             "gbbfs_bfs_device": (I, [P, i32, I, I, I, P]),
             "gbbfs_results": (I, [P, P, P]),
             "gbbfs_result_device_ptrs": (I, [P, PP, PP]),
@@ -433,6 +434,15 @@ def bc_bfs(g, source):
                               _p(starts), ctypes.byref(levels)), "bc_bfs")
     lv = levels.value
     return sigma, dep, succ[:(m + 31) // 32], order[:int(starts[lv])], starts[:lv + 1]
+
+
+def bc(g, sources):
+    """Approximate betweenness centrality over `sources` (Brandes,
+    src/bc.cc:106-171): float32[n] scores divided by their maximum."""
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    scores = np.empty(g.n, np.float32)
+    _check(lib().gbbfs_bc(g.handle, _p(src), len(src), _p(scores)), "bc")
+    return scores
 
 
 def bfs_device(g, source, alpha=15, beta=18, want_depth=False, stats=False, instrument=False,

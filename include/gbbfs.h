@@ -173,6 +173,16 @@ int gbbfs_result_device_ptrs(gbbfs_graph* g, const int32_t** parent,
 int gbbfs_bc_bfs(gbbfs_graph* g, int32_t source, uint64_t* path_counts, int32_t* depth,
                  uint32_t* succ, int32_t* order, int64_t* level_start, int32_t* levels);
 
+/* Approximate betweenness centrality, Brandes' algorithm over k sources
+ * (src/bc.cc:106-171): for each source the BFS phase above, then the
+ * dependencies from the deepest level up (delta[u] = sum over successor
+ * edges of path_counts[u] / path_counts[v] * (1 + delta[v])) added to the
+ * scores.  scores_out (host, n floats) receives the scores divided by their
+ * maximum, as the reference returns them.  Float sums run in another order
+ * than the reference's, so scores agree to the tolerance its verifier uses
+ * (1e-6 on the normalized scores), not bit for bit. */
+int gbbfs_bc(gbbfs_graph* g, const int32_t* sources, int64_t k, float* scores_out);
+
 /* ---- Batched multi-source BFS (no reference counterpart) ----
  * Many sources of one graph at once, 32, 64 or 128 per batch as a bitmask per
  * vertex, in one persistent kernel per batch captured in a CUDA graph.  Its

@@ -63,3 +63,28 @@ def test_offset64_path(native, oracle, monkeypatch):
     with native.Graph(off, nbr) as g:
         for s in native.pick_sources(off, 3):
             check(native, oracle, off, nbr, g, s)
+
+
+@pytest.mark.parametrize("scale,uniform,k", [(12, False, 16), (12, True, 16), (15, False, 8)])
+def test_brandes_scores(native, oracle, scale, uniform, k):
+    """Normalized scores within the reference verifier's tolerance (1e-6)."""
+    off, nbr = native.make_graph(scale, 16, uniform)
+    srcs = native.pick_sources(off, k)
+    with native.Graph(off, nbr) as g:
+        got = native.bc(g, srcs)
+        again = native.bc(g, srcs)
+    want = oracle.bc(off, nbr, srcs)
+    assert np.array_equal(got, again)                 # deterministic
+    assert float(np.max(np.abs(got - want))) < 1e-6
+    assert got.max() == 1.0
+
+
+def test_brandes_handmade(native, oracle):
+    edges = [[0, 1], [0, 2], [1, 3], [2, 3], [3, 4], [6, 0]] + [[6, 7 + i] for i in range(300)]
+    off, nbr = native.build_csr(np.array(edges, np.int32), num_nodes=400)
+    srcs = np.array([0, 4, 6, 9, 399], np.int32)
+    with native.Graph(off, nbr) as g:
+        got = native.bc(g, srcs)
+        with pytest.raises(native.GbbfsError):
+            native.bc(g, np.array([0, 1000], np.int32))
+    assert float(np.max(np.abs(got - oracle.bc(off, nbr, srcs)))) < 1e-6

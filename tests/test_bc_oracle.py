@@ -59,3 +59,30 @@ def test_bc_bfs_oracle_handmade(oracle):
     assert list(sig) == [1, 1, 1, 2, 2, 0]
     assert int(succ[0]) == (1 << 0) | (1 << 1) | (1 << 3) | (1 << 5) | (1 << 8)
     assert list(starts) == [0, 1, 3, 4, 5]
+
+
+def python_brandes(off, nbr, sources):
+    n = len(off) - 1
+    scores = np.zeros(n, np.float64)
+    for s in sources:
+        sigma, depth, succ, levels = python_bc_bfs(off, nbr, int(s))
+        delta = np.zeros(n, np.float64)
+        for lv in reversed(levels):
+            for u in lv:
+                acc = 0.0
+                for e in range(off[u], off[u + 1]):
+                    v = nbr[e]
+                    if depth[v] == depth[u] + 1:
+                        acc += float(sigma[u]) / float(sigma[v]) * (1.0 + delta[v])
+                delta[u] = acc
+                scores[u] += acc
+    return scores / scores.max()
+
+
+@pytest.mark.parametrize("scale,uniform", [(8, False), (9, True)])
+def test_brandes_oracle_matches_definition(oracle, scale, uniform):
+    off, nbr = oracle.build_synthetic(scale, 8, uniform)
+    srcs = oracle.source_picker(off, 6)
+    got = oracle.bc(off, nbr, srcs)
+    want = python_brandes(off, nbr, srcs)
+    assert np.max(np.abs(got - want)) < 1e-6
