@@ -388,34 +388,48 @@ int32_t orc_bc_bfs(const int64_t* off, const int32_t* nbr, int64_t n, int32_t so
 // above): per source, dependencies from the deepest level up, each term
 // (double)path_counts[u] / (double)path_counts[v] * (1 + delta[v]) added to a
 // float delta as the DMM code does, delta added to the score; the scores are
-// divided by their maximum at the end.
+// divided by their maximum at the end.  precise != 0 keeps deltas and scores
+// in double instead (the exact values the float sums approximate).
 void orc_bc(const int64_t* off, const int32_t* nbr, int64_t n, const int32_t* sources,
-            int64_t k, float* scores) {
+            int64_t k, int precise, float* scores) {
   const int64_t m = off[n];
   std::vector<uint64_t> sigma(n);
   std::vector<int32_t> depth(n), order(n > 0 ? n : 1);
   std::vector<int64_t> starts(n + 2);
   std::vector<uint32_t> succ((m + 31) / 32 + 1);
   std::vector<float> delta(n);
+  std::vector<double> ddelta(n), dscore(n, 0.0);
   for (int64_t v = 0; v < n; v++) scores[v] = 0.0f;
   for (int64_t i = 0; i < k; i++) {
     const int32_t levels = orc_bc_bfs(off, nbr, n, sources[i], sigma.data(), depth.data(),
                                       succ.data(), order.data(), starts.data());
     std::fill(delta.begin(), delta.end(), 0.0f);
+    std::fill(ddelta.begin(), ddelta.end(), 0.0);
     for (int32_t d = levels - 1; d >= 0; d--) {
       for (int64_t it = starts[d]; it < starts[d + 1]; it++) {
         const int32_t u = order[it];
         float delta_u = 0;
+        double ddelta_u = 0;
         for (int64_t e = off[u]; e < off[u + 1]; e++) {
           if ((succ[e >> 5] >> (e & 31)) & 1u) {
             const int32_t v = nbr[e];
-            delta_u += ((double)sigma[u] / (double)sigma[v]) * (1 + delta[v]);
+            const double r = (double)sigma[u] / (double)sigma[v];
+            delta_u += r * (1 + delta[v]);
+            ddelta_u += r * (1 + ddelta[v]);
           }
         }
         delta[u] = delta_u;
         scores[u] += delta_u;
+        ddelta[u] = ddelta_u;
+        dscore[u] += ddelta_u;
       }
     }
+  }
+  if (precise) {
+    double big = 0;
+    for (int64_t v = 0; v < n; v++) big = std::max(big, dscore[v]);
+    for (int64_t v = 0; v < n; v++) scores[v] = (float)(dscore[v] / big);
+    return;
   }
   float biggest = 0;
   for (int64_t v = 0; v < n; v++) biggest = std::max(biggest, scores[v]);

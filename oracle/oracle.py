@@ -47,7 +47,7 @@ def lib():
         L.orc_verify.argtypes = [P, P, i64, ctypes.c_int32, P, ctypes.POINTER(ctypes.c_int)]
         L.orc_alg_bytes.restype = i64
         L.orc_alg_bytes.argtypes = [i64, P, ctypes.c_int]
-        L.orc_bc.argtypes = [P, P, i64, P, i64, P]
+        L.orc_bc.argtypes = [P, P, i64, P, i64, ctypes.c_int, P]
         L.orc_bc_bfs.restype = ctypes.c_int32
         L.orc_bc_bfs.argtypes = [P, P, i64, ctypes.c_int32, P, P, P, P, P]
         _lib = L
@@ -204,12 +204,14 @@ def bc_bfs(off, nbr, source):
     return sigma, dep, succ[:(len(nbr) + 31) // 32], order[:reached], starts[:levels + 1]
 
 
-def bc(off, nbr, sources):
+def bc(off, nbr, sources, precise=False):
     """Brandes over `sources` (src/bc.cc:106-171), serial: float32[n] scores
-    divided by their maximum."""
+    divided by their maximum.  precise=True sums in double throughout (the
+    values the reference's float sums approximate)."""
     off = np.ascontiguousarray(off, dtype=np.int64)
     nbr = np.ascontiguousarray(nbr, dtype=np.int32)
     src = np.ascontiguousarray(sources, dtype=np.int32)
     scores = np.empty(len(off) - 1, np.float32)
-    lib().orc_bc(_ptr(off), _ptr(nbr), len(off) - 1, _ptr(src), len(src), _ptr(scores))
+    lib().orc_bc(_ptr(off), _ptr(nbr), len(off) - 1, _ptr(src), len(src), 1 if precise else 0,
+                 _ptr(scores))
     return scores

@@ -67,13 +67,15 @@ def test_offset64_path(native, oracle, monkeypatch):
 
 @pytest.mark.parametrize("scale,uniform,k", [(12, False, 16), (12, True, 16), (15, False, 8)])
 def test_brandes_scores(native, oracle, scale, uniform, k):
-    """Normalized scores within the reference verifier's tolerance (1e-6)."""
+    """Normalized scores within the reference verifier's tolerance (1e-6) of
+    the exact (double) Brandes sums.  The reference's own float accumulation
+    strays up to ~1.5e-6 from them at this size, so it is not the yardstick."""
     off, nbr = native.make_graph(scale, 16, uniform)
     srcs = native.pick_sources(off, k)
     with native.Graph(off, nbr) as g:
         got = native.bc(g, srcs)
         again = native.bc(g, srcs)
-    want = oracle.bc(off, nbr, srcs)
+    want = oracle.bc(off, nbr, srcs, precise=True)
     assert np.array_equal(got, again)                 # deterministic
     assert float(np.max(np.abs(got - want))) < 1e-6
     assert got.max() == 1.0
@@ -87,4 +89,4 @@ def test_brandes_handmade(native, oracle):
         got = native.bc(g, srcs)
         with pytest.raises(native.GbbfsError):
             native.bc(g, np.array([0, 1000], np.int32))
-    assert float(np.max(np.abs(got - oracle.bc(off, nbr, srcs)))) < 1e-6
+    assert float(np.max(np.abs(got - oracle.bc(off, nbr, srcs, precise=True)))) < 1e-6
