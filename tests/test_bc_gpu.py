@@ -90,3 +90,11 @@ def test_brandes_handmade(native, oracle):
         with pytest.raises(native.GbbfsError):
             native.bc(g, np.array([0, 1000], np.int32))
     assert float(np.max(np.abs(got - oracle.bc(off, nbr, srcs, precise=True)))) < 1e-6
+
+
+def test_bc_cli(native, capsys):
+    from dist_mem_gapbs_gb300 import bc_cli
+    assert bc_cli.main(["-g", "11", "-n", "3"]) == 0
+    out = capsys.readouterr().out
+    assert out.count("source: ") == 3 and "Brandes over 3 sources" in out
+    assert out.strip().splitlines()[-5].endswith(":1")      # the top score is the maximum
