@@ -22,7 +22,8 @@
 // equal the serial restatement exactly; only the order of vertices inside a
 // level depends on timing, as in the reference.
 //
-// Back-propagation walks the levels from the deepest up, a warp per vertex:
+// Back-propagation walks the levels from the deepest up (a thread per vertex
+// of small degree, a warp per larger one):
 // a vertex's dependency sums path_counts[u] / path_counts[v] * (1 + delta[v])
 // over its successor edges (terms in double, as the DMM code computes them,
 // summed in a fixed order), and is added to its score.  Scores are divided by
@@ -171,8 +172,36 @@ __global__ void __launch_bounds__(kThreads) k_bc_expand(
 
 // Dependencies of one level (src/bc.cc:129-152, gapbs-verify/bc.cc:128-141):
 // for u in the level, delta[u] = sum over u's successor edges (u, v) of
-// path_counts[u] / path_counts[v] * (1 + delta[v]), added to u's score.  A
-// warp per vertex; terms in double, summed in a fixed lane order.
+// path_counts[u] / path_counts[v] * (1 + delta[v]), added to u's score.
+// Terms in double, summed in a fixed order.  Vertices of degree up to
+// kBcBackSmall take a thread each (k_bc_back_small, edges in order); larger
+// ones a warp each (k_bc_back, lane-strided, then a fixed shuffle tree).
+constexpr int kBcBackSmall = 32;
+
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_bc_back_small(const OffT* off, const int32_t* nbr,
+                                                            const uint32_t* succ,
+                                                            const unsigned long long* sigma,
+                                                            const int32_t* level, int64_t count,
+                                                            float* delta, float* score) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t u = level[i];
+    const uint64_t b = (uint64_t)off[u], e = (uint64_t)off[u + 1];
+    if (e - b > (uint64_t)kBcBackSmall) continue;
+    const double su = (double)sigma[u];
+    double sum = 0.0;
+    for (uint64_t j = b; j < e; j++) {
+      if ((__ldg(succ + (j >> 5)) >> (j & 31)) & 1u) {
+        const int32_t v = nbr[j];
+        sum += su / (double)sigma[v] * (1.0 + (double)delta[v]);
+      }
+    }
+    delta[u] = (float)sum;
+    score[u] += (float)sum;
+  }
+}
+
 template <typename OffT>
 __global__ void __launch_bounds__(kThreads) k_bc_back(const OffT* off, const int32_t* nbr,
                                                       const uint32_t* succ,
@@ -185,6 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_bc_back(const OffT* off, const int
   for (int64_t i = warp; i < count; i += nwarps) {
     const int32_t u = level[i];
     const uint64_t b = (uint64_t)off[u], e = (uint64_t)off[u + 1];
+    if (e - b <= (uint64_t)kBcBackSmall) continue;
     const double su = (double)sigma[u];
     double sum = 0.0;
     for (uint64_t j = b + lane; j < e; j += 32) {
@@ -302,6 +332,9 @@ int run_brandes(gbbfs_graph* g, const int32_t* sources, int64_t k) {
     GB_CUDA(cudaMemsetAsync(b->delta, 0, 4 * (size_t)g->n, s));
     for (int64_t d = (int64_t)starts.size() - 2; d >= 0; d--) {
       const int64_t count = starts[d + 1] - starts[d];
+      k_bc_back_small<OffT><<<g->sms * 8, kThreads, 0, s>>>(off, g->nbr, b->succ, b->sigma,
+                                                             b->queue + starts[d], count,
+                                                             b->delta, b->score);
       k_bc_back<OffT><<<g->sms * 8, kThreads, 0, s>>>(off, g->nbr, b->succ, b->sigma,
                                                        b->queue + starts[d], count, b->delta,
                                                        b->score);
