@@ -23,7 +23,7 @@
 // level depends on timing, as in the reference.
 //
 // Back-propagation walks the levels from the deepest up (a thread per vertex
-// of small degree, a warp per larger one):
+// of small degree, a warp per larger one, a block per hub):
 // a vertex's dependency sums path_counts[u] / path_counts[v] * (1 + delta[v])
 // over its successor edges (terms in double, as the DMM code computes them,
 // summed in a fixed order), and is added to its score.  Scores are divided by
@@ -175,8 +175,10 @@ __global__ void __launch_bounds__(kThreads) k_bc_expand(
 // path_counts[u] / path_counts[v] * (1 + delta[v]), added to u's score.
 // Terms in double, summed in a fixed order.  Vertices of degree up to
 // kBcBackSmall take a thread each (k_bc_back_small, edges in order); larger
-// ones a warp each (k_bc_back, lane-strided, then a fixed shuffle tree).
+// ones a warp each (k_bc_back, lane-strided, then a fixed shuffle tree), and
+// those above kBcBackHub a block each (k_bc_back_hub).
 constexpr int kBcBackSmall = 32;
+constexpr int kBcBackHub = 2048;   // above this degree a block per vertex
 
 template <typename OffT>
 __global__ void __launch_bounds__(kThreads) k_bc_back_small(const OffT* off, const int32_t* nbr,
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(kThreads) k_bc_back(const OffT* off, const int
   for (int64_t i = warp; i < count; i += nwarps) {
     const int32_t u = level[i];
     const uint64_t b = (uint64_t)off[u], e = (uint64_t)off[u + 1];
-    if (e - b <= (uint64_t)kBcBackSmall) continue;
+    if (e - b <= (uint64_t)kBcBackSmall || e - b > (uint64_t)kBcBackHub) continue;
     const double su = (double)sigma[u];
     double sum = 0.0;
     for (uint64_t j = b + lane; j < e; j += 32) {
@@ -229,6 +231,41 @@ __global__ void __launch_bounds__(kThreads) k_bc_back(const OffT* off, const int
       delta[u] = (float)sum;
       score[u] += (float)sum;
     }
+  }
+}
+
+// Vertices above kBcBackHub: a block each, thread-strided over the edges,
+// then a fixed-order tree over the block.
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_bc_back_hub(const OffT* off, const int32_t* nbr,
+                                                          const uint32_t* succ,
+                                                          const unsigned long long* sigma,
+                                                          const int32_t* level, int64_t count,
+                                                          float* delta, float* score) {
+  __shared__ double part[kThreads];
+  for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+    const int32_t u = level[i];
+    const uint64_t b = (uint64_t)off[u], e = (uint64_t)off[u + 1];
+    if (e - b <= (uint64_t)kBcBackHub) continue;   // block-uniform
+    const double su = (double)sigma[u];
+    double sum = 0.0;
+    for (uint64_t j = b + threadIdx.x; j < e; j += blockDim.x) {
+      if ((__ldg(succ + (j >> 5)) >> (j & 31)) & 1u) {
+        const int32_t v = nbr[j];
+        sum += su / (double)sigma[v] * (1.0 + (double)delta[v]);
+      }
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      delta[u] = (float)part[0];
+      score[u] += (float)part[0];
+    }
+    __syncthreads();
   }
 }
 
@@ -338,6 +375,9 @@ int run_brandes(gbbfs_graph* g, const int32_t* sources, int64_t k) {
       k_bc_back<OffT><<<g->sms * 8, kThreads, 0, s>>>(off, g->nbr, b->succ, b->sigma,
                                                        b->queue + starts[d], count, b->delta,
                                                        b->score);
+      k_bc_back_hub<OffT><<<g->sms * 8, kThreads, 0, s>>>(off, g->nbr, b->succ, b->sigma,
+                                                           b->queue + starts[d], count, b->delta,
+                                                           b->score);
       GB_CUDA(cudaGetLastError());
     }
   }
