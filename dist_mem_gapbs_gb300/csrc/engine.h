@@ -43,6 +43,11 @@ void* ms_depth(gbbfs_graph* g, int buf);           // device rows of `buf`
 cudaEvent_t ms_done_event(gbbfs_graph* g, int buf);
 void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s);  // copies out of `buf` queued on s
 
+// Stable LSD radix sort of len 64-bit keys on their low key_bits bits
+// (gpu_build.cu); keys and tmp hold len each, *out is the sorted one.
+int radix_sort64(uint64_t* keys, uint64_t* tmp, int64_t len, int key_bits, cudaStream_t s,
+                 uint64_t** out);
+
 // A handle from a CSR in device memory (bfs_engine.cu): offsets int64[n+1]
 // and neighbours int32[m], copied into the handle.
 int graph_create_device(const int64_t* d_off, const int32_t* d_nbr, int64_t n, int64_t m,

@@ -37,6 +37,14 @@ constexpr int kRadixTile = kRadixThreads * kRadixRounds;   // keys per block
 constexpr int kRadixWarps = kRadixThreads / 32;
 constexpr int kDigits = 256;
 
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() { cudaFree(p); }
+  template <typename T>
+  T* as() { return static_cast<T*>(p); }
+};
+
+
 // ---------------------------------------------------------------------------
 // Radix sort of 64-bit keys.
 
@@ -95,6 +103,39 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint64_t*
     if (valid) out[gbase[d] + wbase[w][d] + lrank] = key;
   }
 }
+
+}  // namespace
+
+// Sort len 64-bit keys on their low key_bits bits, stably (LSD, 8-bit
+// digits).  keys and tmp hold len entries each; *out is the one that ends up
+// holding the sorted keys.
+int radix_sort64(uint64_t* keys, uint64_t* tmp, int64_t len, int key_bits, cudaStream_t s,
+                 uint64_t** out) {
+  *out = keys;
+  if (len <= 0) return GBBFS_OK;
+  const int64_t tiles = (len + kRadixTile - 1) / kRadixTile;
+  DevBuf counts, starts;
+  GB_CUDA(cudaMalloc(&counts.p, sizeof(int32_t) * kDigits * (size_t)tiles));
+  GB_CUDA(cudaMalloc(&starts.p, sizeof(int64_t) * kDigits * (size_t)tiles));
+  uint64_t* src = keys;
+  uint64_t* dst = tmp;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    k_radix_count<<<(unsigned)tiles, kRadixThreads, 0, s>>>(src, len, shift, tiles,
+                                                             counts.as<int32_t>());
+    GB_CUDA(cudaGetLastError());
+    GB_TRY(device_scan<int32_t>(counts.as<int32_t>(), kDigits * tiles, starts.as<int64_t>(),
+                                false, s));
+    k_radix_scatter<<<(unsigned)tiles, kRadixThreads, 0, s>>>(src, dst, len, shift, tiles,
+                                                               starts.as<int64_t>());
+    GB_CUDA(cudaGetLastError());
+    std::swap(src, dst);
+  }
+  GB_CUDA(cudaStreamSynchronize(s));
+  *out = src;
+  return GBBFS_OK;
+}
+
+namespace {
 
 // ---------------------------------------------------------------------------
 // Edge list -> keys, and the squish of the sorted keys.
@@ -191,13 +232,6 @@ int bit_length64(uint64_t x) {
   return b;
 }
 
-struct DevBuf {
-  void* p = nullptr;
-  ~DevBuf() { cudaFree(p); }
-  template <typename T>
-  T* as() { return static_cast<T*>(p); }
-};
-
 // The squished CSR of the edge list in device memory.
 int build_on_device(const int32_t* el_pairs, int64_t edges, int64_t num_nodes, cudaStream_t s,
                     DevBuf* off_out, DevBuf* nbr_out, int64_t* n_out, int64_t* m_out) {
@@ -257,23 +291,8 @@ int build_on_device(const int32_t* el_pairs, int64_t edges, int64_t num_nodes, c
     cudaFree(el.p);
     el.p = nullptr;
     // LSD radix sort over the 2 * bits key bits.
-    const int64_t tiles = (len + kRadixTile - 1) / kRadixTile;
-    DevBuf counts, starts;
-    GB_CUDA(cudaMalloc(&counts.p, sizeof(int32_t) * kDigits * (size_t)tiles));
-    GB_CUDA(cudaMalloc(&starts.p, sizeof(int64_t) * kDigits * (size_t)tiles));
-    uint64_t* src = a.as<uint64_t>();
-    uint64_t* dst = b.as<uint64_t>();
-    for (int shift = 0; shift < 2 * bits; shift += 8) {
-      k_radix_count<<<(unsigned)tiles, kRadixThreads, 0, s>>>(src, len, shift, tiles,
-                                                               counts.as<int32_t>());
-      GB_CUDA(cudaGetLastError());
-      GB_TRY(device_scan<int32_t>(counts.as<int32_t>(), kDigits * tiles, starts.as<int64_t>(),
-                                  false, s));
-      k_radix_scatter<<<(unsigned)tiles, kRadixThreads, 0, s>>>(src, dst, len, shift, tiles,
-                                                                 starts.as<int64_t>());
-      GB_CUDA(cudaGetLastError());
-      std::swap(src, dst);
-    }
+    uint64_t* src = nullptr;
+    GB_TRY(radix_sort64(a.as<uint64_t>(), b.as<uint64_t>(), len, 2 * bits, s, &src));
     // Squish: kept keys per tile, their positions, the neighbour ids.
     const int64_t stiles = (len + kSquishTile - 1) / kSquishTile;
     DevBuf tile_kept, tile_base;

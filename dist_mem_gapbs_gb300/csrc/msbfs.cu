@@ -178,9 +178,12 @@ const void* kernel_for(const gbbfs_graph* g, const MsConfig& cfg, int depth_byte
 // first, in id order inside each bucket; then the others in id order (a
 // counting sort on the host over the offsets).  Inside a bucket vertices keep
 // their order, so the rows put back into original order read from a few
-// sequential runs.  The neighbour lists are then copied and renamed on the
-// device.  Hubs (degree above kMsHubDeg) are listed in new-id order with
-// their work chunks' prefix.
+// sequential runs.  The neighbour lists are then renamed and sorted by new
+// id on the device (a radix sort of the directed edges' (new u, new v) keys),
+// so every list starts with its highest-degree neighbours: they are in many
+// sources' frontiers at once, and bottom-up scans that stop once every lane
+// is found stop sooner.  Hubs (degree above kMsHubDeg) are listed in new-id
+// order with their work chunks' prefix.
 template <typename OffT, typename Alloc>
 int build_order(gbbfs_graph* g, MsState* ms, Alloc&& alloc) {
   const int64_t n = g->n;
@@ -251,21 +254,36 @@ int build_order(gbbfs_graph* g, MsState* ms, Alloc&& alloc) {
   GB_TRY(alloc(&ms->roff, sizeof(OffT) * (size_t)(n + 1)));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->rnbr), 4 * (size_t)g->m));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->perm), 4 * (size_t)n));
-  int32_t* d_inv = nullptr;
-  GB_CUDA(cudaMalloc(&d_inv, 4 * (size_t)n));
   cudaError_t e = cudaMemcpy(ms->roff, noff.data(), sizeof(OffT) * (size_t)(n + 1),
                              cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(ms->perm, perm.data(), 4 * (size_t)n, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(d_inv, inv.data(), 4 * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && g->m > 0) {
-    k_relabel_nbr<OffT><<<4 * g->sms, kThreads, 0, g->stream>>>(
-        reinterpret_cast<const OffT*>(g->off), g->nbr, reinterpret_cast<const OffT*>(ms->roff),
-        d_inv, ms->perm, ms->rnbr, n);
-    e = cudaGetLastError();
+    // Neighbour lists renamed and sorted by new id (hubs first): the keys
+    // (new u, new v) of all directed edges, radix-sorted.
+    int bits = 1;
+    while (bits < 31 && (int64_t(1) << bits) < n) bits++;
+    uint64_t *ka = nullptr, *kb = nullptr, *sorted = nullptr;
+    e = cudaMalloc(&ka, 8 * (size_t)g->m);
+    if (e == cudaSuccess) e = cudaMalloc(&kb, 8 * (size_t)g->m);
+    if (e == cudaSuccess) {
+      k_relabel_keys<OffT><<<8 * g->sms, kThreads, 0, g->stream>>>(
+          reinterpret_cast<const OffT*>(g->off), g->nbr, ms->perm, n, bits, ka);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess &&
+        radix_sort64(ka, kb, g->m, 2 * bits, g->stream, &sorted) != GBBFS_OK)
+      e = cudaErrorUnknown;
+    if (e == cudaSuccess) {
+      k_low_bits<<<8 * g->sms, kThreads, 0, g->stream>>>(sorted, g->m, (1ull << bits) - 1,
+                                                          ms->rnbr);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(ka);
+    cudaFree(kb);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-  cudaFree(d_inv);
   if (e != cudaSuccess) {
     ms_error = std::string("search-ordered graph copy: ") + cudaGetErrorString(e);
     return GBBFS_ERR_CUDA;

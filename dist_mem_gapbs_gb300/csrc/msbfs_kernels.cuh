@@ -943,23 +943,28 @@ __global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<
   if (threadIdx.x < kMsPhases) atomicAdd(&c->phase_cycles[threadIdx.x], ph_acc[threadIdx.x]);
 }
 
-// The search-ordered copy of the CSR: new vertex r is original vertex
-// inv[r], and every neighbour id is mapped through perm.  A warp per vertex.
+// Keys of the search-ordered CSR: (perm[u] << bits) | perm[v] for every
+// directed edge (u, v), at u's edge positions.  Sorted, they list every new
+// vertex's neighbours in new-id order (highest degree first).  A warp per
+// original vertex.
 template <typename OffT>
-__global__ void __launch_bounds__(kThreads) k_relabel_nbr(const OffT* off, const int32_t* nbr,
-                                                          const OffT* noff, const int32_t* inv,
-                                                          const int32_t* perm, int32_t* nnbr,
-                                                          int64_t n) {
+__global__ void __launch_bounds__(kThreads) k_relabel_keys(const OffT* off, const int32_t* nbr,
+                                                           const int32_t* perm, int64_t n,
+                                                           int bits, uint64_t* keys) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = warp; r < n; r += nwarps) {
-    const int32_t u = inv[r];
-    const uint64_t b = (uint64_t)off[u];
-    const uint64_t d = (uint64_t)off[u + 1] - b;
-    const uint64_t nb = (uint64_t)noff[r];
-    for (uint64_t j = lane; j < d; j += 32) nnbr[nb + j] = perm[nbr[b + j]];
+  for (int64_t u = warp; u < n; u += nwarps) {
+    const uint64_t b = (uint64_t)off[u], e = (uint64_t)off[u + 1];
+    const uint64_t hi = (uint64_t)(uint32_t)perm[u] << bits;
+    for (uint64_t j = b + lane; j < e; j += 32) keys[j] = hi | (uint32_t)perm[nbr[j]];
   }
+}
+
+static __global__ void k_low_bits(const uint64_t* keys, int64_t len, uint64_t mask, int32_t* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int32_t)(keys[i] & mask);
 }
 
 // Transpose of a 4x4 byte block: word j of the result holds byte j of each of
