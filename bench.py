@@ -441,7 +441,7 @@ def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
             plain_ms.append(gbbfs.bfs_device(g, int(s), stats=True).device_ms)
         plain_qps = 1e3 / np.mean(plain_ms)
         t0 = time.time()
-        best = gbbfs.msbfs_autotune(g, srcs[:128], 1)     # a full batch at every width
+        best = gbbfs.msbfs_autotune(g, srcs[:384], 1)     # three batches at every width
         tune_s = time.time() - t0
         lanes = best["lanes"]
         gbbfs.msbfs_device(g, srcs[:lanes], 1)          # warm

@@ -739,6 +739,7 @@ int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int d
   static const int kLanes[] = {32, 64, 128};
   static const int kBatches[] = {4, 8, 16};
   static const int kAlphas[] = {2, 6, 15, 40, 200};
+  const int64_t kTuneQueries = 3 * kMsMaxLanes;
   double best_t = 1e300;
   gbbfs_ms_config pick = {64, 8, 15};
   for (int lanes : kLanes)
@@ -746,11 +747,19 @@ int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int d
       for (int alpha : kAlphas) {
         gbbfs_ms_config c = {lanes, batch, alpha};
         GB_TRY(gbbfs_msbfs_set_config(g, &c));
-        const int64_t kk = std::min<int64_t>(k, lanes);
+        // The same queries for every width: up to kTuneQueries of the
+        // sample, in whole batches, so one slow batch does not decide.
+        const int64_t total = k >= lanes ? std::min<int64_t>(k, kTuneQueries) / lanes * lanes : k;
         gbbfs_ms_stats st;
-        GB_TRY(run_batches(g, sample, kk, depth_bytes, nullptr, &st));   // warm
-        GB_TRY(run_batches(g, sample, kk, depth_bytes, nullptr, &st));
-        const double per_query = st.device_ms / (double)kk;
+        GB_TRY(run_batches(g, sample, std::min<int64_t>(total, lanes), depth_bytes, nullptr,
+                           &st));   // warm
+        double ms = 0;
+        for (int64_t b = 0; b < total; b += lanes) {
+          GB_TRY(run_batches(g, sample + b, std::min<int64_t>(lanes, total - b), depth_bytes,
+                             nullptr, &st));
+          ms += st.device_ms;
+        }
+        const double per_query = ms / (double)total;
         if (per_query < best_t) {
           best_t = per_query;
           pick = c;

@@ -238,8 +238,9 @@ int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg);
 int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg);
 
 /* Autotuner: time every configuration of the built-in grid (lanes x batch x
- * alpha) on the given sample sources, keep the fastest per query on the
- * handle and return it in *best. */
+ * alpha) on the given sample sources (up to 384 of them, in whole batches
+ * of each width), keep the fastest per query on the handle and return it in
+ * *best. */
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,
                          gbbfs_ms_config* best);
 
