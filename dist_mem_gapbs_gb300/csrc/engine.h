@@ -42,6 +42,8 @@ int ms_finish(gbbfs_graph* g, int buf);            // wait, then report its stat
 void* ms_depth(gbbfs_graph* g, int buf);           // device rows of `buf`
 cudaEvent_t ms_done_event(gbbfs_graph* g, int buf);
 void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s);  // copies out of `buf` queued on s
+// Indices of sources[0..k) in the order to batch them (gbbfs_msbfs_order).
+int ms_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order);
 
 // Stable LSD radix sort of len 64-bit keys on their low key_bits bits
 // (gpu_build.cu); keys and tmp hold len each, *out is the sorted one.
@@ -101,6 +103,9 @@ struct gbbfs_graph {
   bool result_depth = false;
   gbbfs::MsState* ms = nullptr;
   gbbfs::BcState* bc = nullptr;
+  // Batching key per vertex (host): BFS depth from the highest-degree vertex
+  // (255 = unreached) << 8 | (255 - min(degree, 255)).  Made on first use.
+  std::vector<uint16_t> batch_key;
   // gbbfs_bfs_many: staged parent arrays and their copy-out stream.
   int32_t* stage[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;

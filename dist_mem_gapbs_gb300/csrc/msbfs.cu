@@ -1,4 +1,4 @@
-// Batched multi-source BFS: up to 128 sources per batch as a bitmask per vertex.
+// Batched multi-source BFS: up to 256 sources per batch as a bitmask per vertex.
 //
 // This form has no counterpart in the reference: it answers many BFS queries
 // of the same graph at once.  Its results are defined by the reference's
@@ -30,9 +30,10 @@
 namespace gbbfs {
 
 constexpr int kSrcSlot = kMsMaxLanes + 1;   // per batch buffer: count, then the sources
+constexpr int kLaneClasses = 4;              // lane words of 32 << cls bits
 
 struct MsConfig {
-  int lanes = 128;       // 32, 64 or 128 sources per batch (the widest used)
+  int lanes = 128;       // 32, 64, 128 or 256 sources per batch (the widest used)
   int batch = 8;         // neighbours per bottom-up round of one thread
   int alpha = 15;        // top-down while frontier degrees <= m / alpha
 };
@@ -71,10 +72,11 @@ struct MsState {
   cudaEvent_t computed[2] = {nullptr, nullptr};
   cudaEvent_t copied[2] = {nullptr, nullptr};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // One captured graph per batch buffer and lane width (32, 64, 128); the
-  // source count is read on the device, so a graph serves every batch size.
-  cudaGraphExec_t exec[2][3] = {};
-  MsConfig exec_cfg[2][3];
+  // One captured graph per batch buffer and lane width (32, 64, 128, 256);
+  // the source count is read on the device, so a graph serves every batch
+  // size.
+  cudaGraphExec_t exec[2][kLaneClasses] = {};
+  MsConfig exec_cfg[2][kLaneClasses];
   MsConfig cfg;
   int64_t bytes = 0;
   int last_buf = -1;
@@ -84,7 +86,7 @@ struct MsState {
 void msbfs_release(MsState* ms) {
   if (!ms) return;
   for (int i = 0; i < 2; i++) {
-    for (int c = 0; c < 3; c++)
+    for (int c = 0; c < kLaneClasses; c++)
       if (ms->exec[i][c]) cudaGraphExecDestroy(ms->exec[i][c]);
     cudaFree(ms->q[i]);
     cudaFree(ms->qe[i]);
@@ -123,7 +125,7 @@ void msbfs_release(MsState* ms) {
 // ---------------------------------------------------------------------------
 // Host side.
 
-// Lane words are allocated at 128 bits so every lane width fits: visit, the
+// Lane words are allocated at 256 bits so every lane width fits: visit, the
 // two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
 // and tq; two frontier unions and the work-unit table; the search-ordered CSR (offsets counted at 8
 // bytes) and its permutation; the per-vertex depth log (kLogSlots lane masks,
@@ -131,9 +133,9 @@ void msbfs_release(MsState* ms) {
 // cannot hold and two buffers of rows in original order; slack for the hub
 // list and control blocks.
 size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes) {
-  return 4 * 16 * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n + 12 * (size_t)(W + 1) +
-         8 * (size_t)(n + 1) + 4 * (size_t)m + 4 * (size_t)n +
-         (kLogSlots * sizeof(Lane128) + 9) * (size_t)n +
+  return 4 * sizeof(Lane256) * (size_t)n + 2 * 8 * (size_t)n + 3 * 4 * (size_t)n +
+         12 * (size_t)(W + 1) + 8 * (size_t)(n + 1) + 4 * (size_t)m + 4 * (size_t)n +
+         (kLogSlots * sizeof(Lane256) + 9) * (size_t)n +
          3 * (size_t)kMsMaxLanes * (n + kDepthTile) * depth_bytes + (16 << 20);
 }
 
@@ -163,6 +165,7 @@ const void* pick_depth(int depth_bytes, int batch) {
 
 template <typename OffT>
 const void* pick_kernel(const MsConfig& cfg, int depth_bytes) {
+  if (cfg.lanes == 256) return pick_depth<OffT, Lane256>(depth_bytes, cfg.batch);
   if (cfg.lanes == 128) return pick_depth<OffT, Lane128>(depth_bytes, cfg.batch);
   return cfg.lanes == 32 ? pick_depth<OffT, uint32_t>(depth_bytes, cfg.batch)
                          : pick_depth<OffT, unsigned long long>(depth_bytes, cfg.batch);
@@ -171,6 +174,83 @@ const void* pick_kernel(const MsConfig& cfg, int depth_bytes) {
 const void* kernel_for(const gbbfs_graph* g, const MsConfig& cfg, int depth_bytes) {
   return g->off32 ? pick_kernel<uint32_t>(cfg, depth_bytes)
                   : pick_kernel<unsigned long long>(cfg, depth_bytes);
+}
+
+// Batching keys.  A batch costs about as many full bottom-up levels as its
+// slowest source needs, so sources that reach the bulk of the graph at the
+// same level should share a batch.  The proxy for that level is the source's
+// BFS depth from the highest-degree vertex; among sources at the same depth,
+// higher degree reaches the bulk sooner.
+template <typename OffT>
+__global__ void k_argmax_degree(const OffT* off, int64_t n, unsigned long long* best) {
+  unsigned long long mine = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long d = (unsigned long long)(off[v + 1] - off[v]);
+    const unsigned long long key = ((d < 0xffffffffull ? d : 0xffffffffull) << 32) |
+                                   (0xffffffffull - (unsigned long long)v);   // lowest id wins ties
+    mine = mine > key ? mine : key;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(kFull, mine, o);
+    mine = mine > x ? mine : x;
+  }
+  if ((threadIdx.x & 31) == 0 && mine) atomicMax(best, mine);
+}
+
+template <typename OffT>
+__global__ void k_batch_keys(const OffT* off, const int32_t* depth, int64_t n, uint16_t* keys) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t d = depth[v];
+    const uint32_t hd = d < 0 ? 255u : d > 254 ? 254u : (uint32_t)d;
+    const unsigned long long deg = (unsigned long long)(off[v + 1] - off[v]);
+    keys[v] = (uint16_t)((hd << 8) | (255u - (uint32_t)(deg < 255 ? deg : 255)));
+  }
+}
+
+template <typename OffT>
+int make_batch_keys(gbbfs_graph* g) {
+  const int64_t n = g->n;
+  const OffT* off = reinterpret_cast<const OffT*>(g->off);
+  unsigned long long* d_best = nullptr;
+  uint16_t* d_keys = nullptr;
+  GB_CUDA(cudaMalloc(&d_best, sizeof(unsigned long long)));
+  cudaError_t e = cudaMalloc(&d_keys, 2 * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_best, 0, sizeof(unsigned long long), g->stream);
+  if (e == cudaSuccess) {
+    k_argmax_degree<OffT><<<4 * g->sms, kThreads, 0, g->stream>>>(off, n, d_best);
+    e = cudaGetLastError();
+  }
+  unsigned long long best = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&best, d_best, sizeof best, cudaMemcpyDeviceToHost, g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  int rc = GBBFS_OK;
+  if (e == cudaSuccess) {
+    const int32_t hub = (int32_t)(0xffffffffull - (best & 0xffffffffull));
+    rc = gbbfs_bfs_device(g, hub, 0, 0, 1, nullptr);
+    const int32_t* depth = nullptr;
+    if (rc == GBBFS_OK) rc = gbbfs_result_device_ptrs(g, nullptr, &depth);
+    if (rc == GBBFS_OK) {
+      k_batch_keys<OffT><<<4 * g->sms, kThreads, 0, g->stream>>>(off, depth, n, d_keys);
+      e = cudaGetLastError();
+      std::vector<uint16_t> keys((size_t)n);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(keys.data(), d_keys, 2 * (size_t)n, cudaMemcpyDeviceToHost, g->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+      if (e == cudaSuccess) g->batch_key.swap(keys);
+    }
+  }
+  cudaFree(d_best);
+  cudaFree(d_keys);
+  if (rc != GBBFS_OK) return rc;
+  if (e != cudaSuccess) {
+    ms_error = std::string("batching keys: ") + cudaGetErrorString(e);
+    return GBBFS_ERR_CUDA;
+  }
+  return GBBFS_OK;
 }
 
 // The search-ordered copy of the graph.  New ids: the vertices of degree
@@ -331,17 +411,17 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
     ms->bytes += (int64_t)bytes;
     return GBBFS_OK;
   };
-  GB_TRY(alloc(&ms->visit, sizeof(Lane128) * (size_t)n));
-  GB_TRY(alloc(&ms->fr[0], sizeof(Lane128) * (size_t)n));
-  GB_TRY(alloc(&ms->fr[1], sizeof(Lane128) * (size_t)n));
-  GB_TRY(alloc(&ms->acc, sizeof(Lane128) * (size_t)n));
+  GB_TRY(alloc(&ms->visit, sizeof(Lane256) * (size_t)n));
+  GB_TRY(alloc(&ms->fr[0], sizeof(Lane256) * (size_t)n));
+  GB_TRY(alloc(&ms->fr[1], sizeof(Lane256) * (size_t)n));
+  GB_TRY(alloc(&ms->acc, sizeof(Lane256) * (size_t)n));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[0]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->fbits[1]), 4 * (size_t)g->W));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tq), 4 * (size_t)n));
   ms->dstride = (n + kDepthTile - 1) / kDepthTile * kDepthTile;
   GB_TRY(alloc(&ms->dtmp, (size_t)kMsMaxLanes * ms->dstride * depth_bytes));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->lvl), 4 * (size_t)n));
-  GB_TRY(alloc(&ms->lmask, (size_t)kLogSlots * sizeof(Lane128) * n));
+  GB_TRY(alloc(&ms->lmask, (size_t)kLogSlots * sizeof(Lane256) * n));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->spill), (size_t)n));
   GB_TRY(alloc(reinterpret_cast<void**>(&ms->tflag), 4 * (size_t)n));
   GB_TRY(g->off32 ? build_order<uint32_t>(g, ms, alloc)
@@ -481,6 +561,7 @@ int capture_depth(gbbfs_graph* g, int buf, int cls) {
 
 template <typename OffT>
 int capture_lanes(gbbfs_graph* g, int buf, int cls) {
+  if (cls == 3) return capture_depth<OffT, Lane256>(g, buf, cls);
   if (cls == 2) return capture_depth<OffT, Lane128>(g, buf, cls);
   return cls == 0 ? capture_depth<OffT, uint32_t>(g, buf, cls)
                   : capture_depth<OffT, unsigned long long>(g, buf, cls);
@@ -583,8 +664,10 @@ int check_batch(gbbfs_graph* g, int buf, MsTally* t) {
   return GBBFS_OK;
 }
 
+// Batches of sources[0..k) back to back.  With host_out, the row of
+// sources[j] goes to row row_of[j] of host_out (row j when row_of is null).
 int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
-                void* host_out, gbbfs_ms_stats* st) {
+                void* host_out, gbbfs_ms_stats* st, const int32_t* row_of = nullptr) {
   if (!g || !sources || k <= 0 || (depth_bytes != 1 && depth_bytes != 4)) {
     ms_error = "bad multi-source arguments";
     return GBBFS_ERR_ARG;
@@ -608,9 +691,16 @@ int run_batches(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
     if (host_out) {
       // Copy this batch out on the copy stream while the next one computes.
       GB_CUDA(cudaStreamWaitEvent(ms->copy_stream, ms->computed[buf], 0));
-      GB_CUDA(cudaMemcpyAsync(static_cast<char*>(host_out) + (size_t)b * lanes * per_src,
-                              ms->depth[buf], (size_t)kb * per_src, cudaMemcpyDeviceToHost,
-                              ms->copy_stream));
+      char* out = static_cast<char*>(host_out);
+      if (!row_of) {
+        GB_CUDA(cudaMemcpyAsync(out + (size_t)b * lanes * per_src, ms->depth[buf],
+                                (size_t)kb * per_src, cudaMemcpyDeviceToHost, ms->copy_stream));
+      } else {
+        for (int j = 0; j < kb; j++)
+          GB_CUDA(cudaMemcpyAsync(out + (size_t)row_of[b * lanes + j] * per_src,
+                                  static_cast<const char*>(ms->depth[buf]) + (size_t)j * per_src,
+                                  per_src, cudaMemcpyDeviceToHost, ms->copy_stream));
+      }
       GB_CUDA(cudaEventRecord(ms->copied[buf], ms->copy_stream));
     }
     if (b >= 1) GB_TRY(check_batch(g, buf ^ 1, &tally));
@@ -679,6 +769,24 @@ void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s) {
   cudaEventRecord(g->ms->copied[buf], s);
 }
 
+int ms_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order) {
+  for (int64_t i = 0; i < k; i++) {
+    if (sources[i] < 0 || sources[i] >= g->n) {
+      ms_error = "source out of range";
+      return GBBFS_ERR_ARG;
+    }
+  }
+  if ((int64_t)g->batch_key.size() != g->n) {
+    GB_CUDA(cudaSetDevice(g->device));
+    GB_TRY(g->off32 ? make_batch_keys<uint32_t>(g) : make_batch_keys<unsigned long long>(g));
+  }
+  for (int64_t i = 0; i < k; i++) order[i] = (int32_t)i;
+  const uint16_t* key = g->batch_key.data();
+  std::stable_sort(order, order + k,
+                   [&](int32_t a, int32_t b) { return key[sources[a]] < key[sources[b]]; });
+  return GBBFS_OK;
+}
+
 }  // namespace gbbfs
 
 using namespace gbbfs;
@@ -687,8 +795,19 @@ extern "C" {
 
 int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
                 void* depth_out, gbbfs_ms_stats* st) {
-  if (!depth_out) return GBBFS_ERR_ARG;
-  return run_batches(g, sources, k, depth_bytes, depth_out, st);
+  if (!g || !sources || !depth_out || k <= 0) return GBBFS_ERR_ARG;
+  if (k <= ms_lanes(g)) return run_batches(g, sources, k, depth_bytes, depth_out, st);
+  // Several batches: batch the sources in gbbfs_msbfs_order's order; each row
+  // is copied to its caller's position.
+  std::vector<int32_t> order((size_t)k), batched((size_t)k);
+  GB_TRY(ms_order(g, sources, k, order.data()));
+  for (int64_t j = 0; j < k; j++) batched[j] = sources[order[j]];
+  return run_batches(g, batched.data(), k, depth_bytes, depth_out, st, order.data());
+}
+
+int gbbfs_msbfs_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order_out) {
+  if (!g || k < 0 || (k > 0 && (!sources || !order_out))) return GBBFS_ERR_ARG;
+  return ms_order(g, sources, k, order_out);
 }
 
 int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
@@ -702,9 +821,9 @@ int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int de
 
 int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg) {
   if (!g || !cfg) return GBBFS_ERR_ARG;
-  if ((cfg->lanes != 32 && cfg->lanes != 64 && cfg->lanes != 128) ||
+  if ((cfg->lanes != 32 && cfg->lanes != 64 && cfg->lanes != 128 && cfg->lanes != 256) ||
       (cfg->batch != 4 && cfg->batch != 8 && cfg->batch != 16) || cfg->alpha < 1) {
-    last_error() = "lanes must be 32, 64 or 128, batch 4, 8 or 16, alpha >= 1";
+    last_error() = "lanes must be 32, 64, 128 or 256, batch 4, 8 or 16, alpha >= 1";
     return GBBFS_ERR_ARG;
   }
   GB_CUDA(cudaSetDevice(g->device));
@@ -736,10 +855,18 @@ int64_t gbbfs_msbfs_state_bytes(int64_t n, int64_t m_dir, int depth_bytes) {
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,
                          gbbfs_ms_config* best) {
   if (!g || !sample || k <= 0) return GBBFS_ERR_ARG;
-  static const int kLanes[] = {32, 64, 128};
+  // Time batches formed the way gbbfs_msbfs forms them.
+  std::vector<int32_t> order((size_t)k), ordered((size_t)k);
+  GB_TRY(ms_order(g, sample, k, order.data()));
+  for (int64_t j = 0; j < k; j++) ordered[j] = sample[order[j]];
+  sample = ordered.data();
+  static const int kLanes[] = {32, 64, 128, 256};
   static const int kBatches[] = {4, 8, 16};
   static const int kAlphas[] = {2, 6, 15, 40, 200};
-  const int64_t kTuneQueries = 3 * kMsMaxLanes;
+  // The same queries for every width: up to two batches of the widest word
+  // (whole batches of every width), so one slow batch does not decide.
+  int64_t base = std::min<int64_t>(k, 2 * kMsMaxLanes);
+  if (base >= kMsMaxLanes) base -= base % kMsMaxLanes;
   double best_t = 1e300;
   gbbfs_ms_config pick = {64, 8, 15};
   for (int lanes : kLanes)
@@ -747,9 +874,7 @@ int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int d
       for (int alpha : kAlphas) {
         gbbfs_ms_config c = {lanes, batch, alpha};
         GB_TRY(gbbfs_msbfs_set_config(g, &c));
-        // The same queries for every width: up to kTuneQueries of the
-        // sample, in whole batches, so one slow batch does not decide.
-        const int64_t total = k >= lanes ? std::min<int64_t>(k, kTuneQueries) / lanes * lanes : k;
+        const int64_t total = base >= lanes ? base / lanes * lanes : base;
         gbbfs_ms_stats st;
         GB_TRY(run_batches(g, sample, std::min<int64_t>(total, lanes), depth_bytes, nullptr,
                            &st));   // warm

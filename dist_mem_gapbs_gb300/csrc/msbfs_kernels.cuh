@@ -1,6 +1,7 @@
 // Device side of the batched multi-source BFS (sm_103a).
 //
-// Layout in HBM (n vertices, W = ceil(n/32), L = lane word of 32 or 64 bits):
+// Layout in HBM (n vertices, W = ceil(n/32), L = lane word of 32, 64, 128 or
+// 256 bits; a 256-bit word is one 32-byte DRAM sector):
 //   visit      L[n]     bit i set once source i has reached v
 //   fr0/fr1    L[n]     frontier of level l in fr[l & 1]: bit i set if v is in
 //                       the frontier of source i
@@ -61,7 +62,7 @@ constexpr int kMsSmall = 32;        // bottom-up: lower degrees share a streamed
 constexpr int kMsOrderDeg = GBBFS_MS_ORDER_DEG;
 constexpr int kDepthTile = 128;     // rows in search order: stride a multiple of this
 constexpr int kDecodeTile = 64;     // bytes of each row per block of the depth decode
-constexpr int kMsMaxLanes = 128;    // sources per batch at most (depth record length)
+constexpr int kMsMaxLanes = 256;    // sources per batch at most (depth record length)
 constexpr int kMsGrab = 8;          // tiles of 32 vertices in a bottom-up work unit at most
 constexpr int kMsUnitEdges = 4096;  // a unit also ends once its tiles hold this many edges
 constexpr int kMsHubDeg = 4096;
@@ -112,7 +113,7 @@ struct MsArgs {
   uint32_t* lvl;             // per vertex: levels of its kLogSlots log entries (0xff = empty)
   LaneT* lmask;              // per vertex: the lanes each log entry found
   uint8_t* spill;            // per vertex: 1 if some depths are in the rows instead
-  uint32_t* tflag;           // per vertex: touched in this level (128-lane words)
+  uint32_t* tflag;           // per vertex: touched in this level (128/256-lane words)
   const int32_t* nsrc;      // sources in this batch (device, set per launch)
   const int32_t* sources;   // original vertex ids
   const int32_t* perm;      // original id -> search order id
@@ -142,10 +143,48 @@ __device__ __forceinline__ Lane128 shfl(Lane128 x, int src) {
   return {shfl(x.lo, src), shfl(x.hi, src)};
 }
 
-// Lane-word helpers for the three widths (uint32, uint64, Lane128).
+// A lane word of 256 sources (q[0] = sources 0..63): one 32-byte sector, so
+// a random frontier read fetches no bytes it does not use.  Indexes into q
+// are compile-time constants everywhere (a run-time index would put the word
+// in local memory).
+struct __align__(32) Lane256 {
+  unsigned long long q[4];
+  Lane256() = default;
+  __host__ __device__ constexpr Lane256(unsigned long long x) : q{x, 0ull, 0ull, 0ull} {}
+  __host__ __device__ constexpr Lane256(unsigned long long a, unsigned long long b,
+                                        unsigned long long c, unsigned long long d)
+      : q{a, b, c, d} {}
+  __host__ __device__ explicit operator bool() const { return (q[0] | q[1] | q[2] | q[3]) != 0; }
+};
+__host__ __device__ inline Lane256 operator&(Lane256 a, Lane256 b) {
+  return {a.q[0] & b.q[0], a.q[1] & b.q[1], a.q[2] & b.q[2], a.q[3] & b.q[3]};
+}
+__host__ __device__ inline Lane256 operator|(Lane256 a, Lane256 b) {
+  return {a.q[0] | b.q[0], a.q[1] | b.q[1], a.q[2] | b.q[2], a.q[3] | b.q[3]};
+}
+__host__ __device__ inline Lane256 operator~(Lane256 a) { return {~a.q[0], ~a.q[1], ~a.q[2], ~a.q[3]}; }
+__host__ __device__ inline Lane256& operator&=(Lane256& a, Lane256 b) { return a = a & b; }
+__host__ __device__ inline Lane256& operator|=(Lane256& a, Lane256 b) { return a = a | b; }
+__host__ __device__ inline bool operator==(Lane256 a, Lane256 b) {
+  return ((a.q[0] ^ b.q[0]) | (a.q[1] ^ b.q[1]) | (a.q[2] ^ b.q[2]) | (a.q[3] ^ b.q[3])) == 0;
+}
+__host__ __device__ inline bool operator!=(Lane256 a, Lane256 b) { return !(a == b); }
+
+__device__ __forceinline__ Lane256 shfl(Lane256 x, int src) {
+  return {shfl(x.q[0], src), shfl(x.q[1], src), shfl(x.q[2], src), shfl(x.q[3], src)};
+}
+
+// 64-bit word j (0..3) of a 256-lane word, j known only at run time.
+__device__ __forceinline__ unsigned long long word64(const Lane256& x, int j) {
+  return j < 2 ? (j == 0 ? x.q[0] : x.q[1]) : (j == 2 ? x.q[2] : x.q[3]);
+}
+
+// Lane-word helpers for the four widths (uint32, uint64, Lane128, Lane256).
 template <typename LaneT>
 __device__ __forceinline__ uint32_t word32(LaneT x, int h) {   // 32-bit word h
-  if constexpr (sizeof(LaneT) == 16)
+  if constexpr (sizeof(LaneT) == 32)
+    return (uint32_t)(word64(x, h >> 1) >> (32 * (h & 1)));
+  else if constexpr (sizeof(LaneT) == 16)
     return (uint32_t)((h < 2 ? x.lo : x.hi) >> (32 * (h & 1)));
   else
     return (uint32_t)((unsigned long long)x >> (32 * h));
@@ -153,7 +192,10 @@ __device__ __forceinline__ uint32_t word32(LaneT x, int h) {   // 32-bit word h
 
 template <typename LaneT>
 __device__ __forceinline__ LaneT from_words(const uint32_t* w) {
-  if constexpr (sizeof(LaneT) == 16)
+  if constexpr (sizeof(LaneT) == 32)
+    return Lane256(((unsigned long long)w[1] << 32) | w[0], ((unsigned long long)w[3] << 32) | w[2],
+                   ((unsigned long long)w[5] << 32) | w[4], ((unsigned long long)w[7] << 32) | w[6]);
+  else if constexpr (sizeof(LaneT) == 16)
     return Lane128(((unsigned long long)w[1] << 32) | w[0], ((unsigned long long)w[3] << 32) | w[2]);
   else if constexpr (sizeof(LaneT) == 8)
     return (LaneT)(((unsigned long long)w[1] << 32) | w[0]);
@@ -168,7 +210,11 @@ __device__ __forceinline__ bool lane_test(LaneT x, int i) {
 
 template <typename LaneT>
 __device__ __forceinline__ LaneT lane_bit(int i) {
-  if constexpr (sizeof(LaneT) == 16)
+  if constexpr (sizeof(LaneT) == 32) {
+    const unsigned long long b = 1ull << (i & 63);
+    const int j = i >> 6;
+    return Lane256(j == 0 ? b : 0ull, j == 1 ? b : 0ull, j == 2 ? b : 0ull, j == 3 ? b : 0ull);
+  } else if constexpr (sizeof(LaneT) == 16)
     return i < 64 ? Lane128(1ull << i, 0) : Lane128(0, 1ull << (i - 64));
   else
     return (LaneT)((LaneT)1 << i);
@@ -177,7 +223,12 @@ __device__ __forceinline__ LaneT lane_bit(int i) {
 // The k lowest lanes.
 template <typename LaneT>
 __device__ __forceinline__ LaneT lane_ones(int k) {
-  if constexpr (sizeof(LaneT) == 16)
+  if constexpr (sizeof(LaneT) == 32) {
+    auto part = [k](int j) {
+      return k >= 64 * (j + 1) ? ~0ull : k > 64 * j ? (1ull << (k - 64 * j)) - 1 : 0ull;
+    };
+    return Lane256(part(0), part(1), part(2), part(3));
+  } else if constexpr (sizeof(LaneT) == 16)
     return Lane128(k >= 64 ? ~0ull : (1ull << k) - 1,
                    k >= 128 ? ~0ull : k > 64 ? (1ull << (k - 64)) - 1 : 0ull);
   else
@@ -186,7 +237,12 @@ __device__ __forceinline__ LaneT lane_ones(int k) {
 
 template <typename LaneT>
 __device__ __forceinline__ int lowest_bit(LaneT x) {
-  if constexpr (sizeof(LaneT) == 16)
+  if constexpr (sizeof(LaneT) == 32)
+    return x.q[0] ? __ffsll((long long)x.q[0]) - 1
+         : x.q[1] ? 63 + __ffsll((long long)x.q[1])
+         : x.q[2] ? 127 + __ffsll((long long)x.q[2])
+                  : 191 + __ffsll((long long)x.q[3]);
+  else if constexpr (sizeof(LaneT) == 16)
     return x.lo ? __ffsll((long long)x.lo) - 1 : 63 + __ffsll((long long)x.hi);
   else if constexpr (sizeof(LaneT) == 8)
     return __ffsll((long long)x) - 1;
@@ -196,7 +252,13 @@ __device__ __forceinline__ int lowest_bit(LaneT x) {
 
 template <typename LaneT>
 __device__ __forceinline__ LaneT clear_lowest(LaneT x) {
-  if constexpr (sizeof(LaneT) == 16)
+  if constexpr (sizeof(LaneT) == 32) {
+    if (x.q[0]) x.q[0] &= x.q[0] - 1;
+    else if (x.q[1]) x.q[1] &= x.q[1] - 1;
+    else if (x.q[2]) x.q[2] &= x.q[2] - 1;
+    else x.q[3] &= x.q[3] - 1;
+    return x;
+  } else if constexpr (sizeof(LaneT) == 16)
     return x.lo ? Lane128(x.lo & (x.lo - 1), x.hi) : Lane128(0, x.hi & (x.hi - 1));
   else
     return (LaneT)(x & (x - 1));
@@ -205,7 +267,11 @@ __device__ __forceinline__ LaneT clear_lowest(LaneT x) {
 // OR into a lane word in global memory (result not needed).
 template <typename LaneT>
 __device__ __forceinline__ void atomic_or_lane(LaneT* p, LaneT v) {
-  if constexpr (sizeof(LaneT) == 16) {
+  if constexpr (sizeof(LaneT) == 32) {
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (v.q[j]) atomicOr(&p->q[j], v.q[j]);
+  } else if constexpr (sizeof(LaneT) == 16) {
     if (v.lo) atomicOr(&p->lo, v.lo);
     if (v.hi) atomicOr(&p->hi, v.hi);
   } else if constexpr (sizeof(LaneT) == 8) {
@@ -216,11 +282,17 @@ __device__ __forceinline__ void atomic_or_lane(LaneT* p, LaneT v) {
 }
 
 // OR into a lane word; true for the call that first made it non-zero.  A
-// 128-lane word is two 64-bit atomics, so there each half has its own first
-// caller: a word can report two first touches, never none.
+// 128- or 256-lane word is several 64-bit atomics, so there each part has its
+// own first caller: a word can report several first touches, never none.
 template <typename LaneT>
 __device__ __forceinline__ bool first_or_lane(LaneT* p, LaneT v) {
-  if constexpr (sizeof(LaneT) == 16) {
+  if constexpr (sizeof(LaneT) == 32) {
+    bool first = false;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (v.q[j]) first |= atomicOr(&p->q[j], v.q[j]) == 0;
+    return first;
+  } else if constexpr (sizeof(LaneT) == 16) {
     bool first = false;
     if (v.lo) first |= atomicOr(&p->lo, v.lo) == 0;
     if (v.hi) first |= atomicOr(&p->hi, v.hi) == 0;
@@ -233,12 +305,12 @@ __device__ __forceinline__ bool first_or_lane(LaneT* p, LaneT v) {
 }
 
 // OR nb into acc[v]; true for the one call per level that first touched v.
-// 32/64-lane words take it from the atomic's old value; a 128-lane word is
-// two 64-bit atomics, so there a per-vertex flag (cleared by the install)
+// 32/64-lane words take it from the atomic's old value; a wider word is
+// several 64-bit atomics, so there a per-vertex flag (cleared by the install)
 // decides instead.
 template <typename LaneT>
 __device__ __forceinline__ bool touch_or(LaneT* acc, uint32_t* tflag, int64_t v, LaneT nb) {
-  if constexpr (sizeof(LaneT) == 16) {
+  if constexpr (sizeof(LaneT) >= 16) {
     atomic_or_lane(acc + v, nb);
     return atomicOr(tflag + v, 1u) == 0;
   } else {
@@ -268,7 +340,11 @@ __device__ __forceinline__ bool log_found(uint32_t* lvl, LaneT* lmask, int64_t v
 
 template <typename LaneT>
 __device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
-  if constexpr (sizeof(LaneT) == 16) {
+  if constexpr (sizeof(LaneT) == 32) {
+    const ulonglong2 t = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+    const ulonglong2 u = __ldcg(reinterpret_cast<const ulonglong2*>(p) + 1);
+    return Lane256(t.x, t.y, u.x, u.y);
+  } else if constexpr (sizeof(LaneT) == 16) {
     const ulonglong2 t = __ldcg(reinterpret_cast<const ulonglong2*>(p));
     return Lane128(t.x, t.y);
   } else if constexpr (sizeof(LaneT) == 8) {
@@ -282,7 +358,7 @@ __device__ __forceinline__ LaneT ld_lane(const LaneT* p) {
 // per 32-bit word.
 template <typename LaneT>
 __device__ __forceinline__ LaneT group_or(unsigned grp, LaneT x) {
-  uint32_t w[4];
+  uint32_t w[sizeof(LaneT) / 4];
 #pragma unroll
   for (int h = 0; h < (int)(sizeof(LaneT) / 4); h++) w[h] = __reduce_or_sync(grp, word32(x, h));
   return from_words<LaneT>(w);
@@ -461,13 +537,21 @@ __device__ __forceinline__ LaneT warp_gather_or(const int32_t* nbr, const uint32
   return got;
 }
 
-// Resident blocks per SM the register allocation is held to.
+// Resident blocks per SM the register allocation is held to (fewer for the
+// 256-lane word, whose values take twice the registers).
 #ifndef GBBFS_MS_MIN_BLOCKS
 #define GBBFS_MS_MIN_BLOCKS 4
 #endif
+#ifndef GBBFS_MS_MIN_BLOCKS_WIDE
+#define GBBFS_MS_MIN_BLOCKS_WIDE 4
+#endif
+template <typename LaneT>
+constexpr int ms_min_blocks() {
+  return sizeof(LaneT) > 16 ? GBBFS_MS_MIN_BLOCKS_WIDE : GBBFS_MS_MIN_BLOCKS;
+}
 
 template <typename OffT, typename LaneT, typename DepthT, int kBatchN>
-__global__ void __launch_bounds__(kThreads, GBBFS_MS_MIN_BLOCKS) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
+__global__ void __launch_bounds__(kThreads, ms_min_blocks<LaneT>()) k_msbfs(MsArgs<OffT, LaneT, DepthT> a) {
   __shared__ LaneT tile_acc[kWarpsPerCta][32];
   __shared__ int64_t tile_base[kWarpsPerCta][32];
   __shared__ uint8_t tile_owner[kWarpsPerCta][32 * kMsSmall];

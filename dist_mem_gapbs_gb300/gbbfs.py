@@ -35,7 +35,8 @@ EXPORTS = (
     "gbbfs_last_error", "gbbfs_generate", "gbbfs_free_host", "gbbfs_generate_edges",
     "gbbfs_build_csr", "gbbfs_read_graph", "gbbfs_write_sg", "gbbfs_pick_sources",
     "gbbfs_append_bfs_output", "gbbfs_msbfs", "gbbfs_msbfs_device", "gbbfs_msbfs_set_config",
-    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_msbfs_state_bytes", "gbbfs_server_open",
+    "gbbfs_msbfs_get_config", "gbbfs_msbfs_autotune", "gbbfs_msbfs_state_bytes",
+    "gbbfs_msbfs_order", "gbbfs_server_open",
     "gbbfs_server_add_graph", "gbbfs_server_submit", "gbbfs_server_submit_many",
     "gbbfs_server_poll", "gbbfs_server_drain",
     "gbbfs_server_clock", "gbbfs_server_close", "gbbfs_bfs_noalloc",
@@ -141,6 +142,7 @@ def lib():
             "gbbfs_msbfs_get_config": (I, [P, P]),
             "gbbfs_msbfs_autotune": (I, [P, P, i64, I, P]),
             "gbbfs_msbfs_state_bytes": (i64, [i64, i64, I]),
+            "gbbfs_msbfs_order": (I, [P, P, i64, P]),
             "gbbfs_server_open": (I, [P, PP]),
             "gbbfs_server_add_graph": (I, [P, P, P]),
             "gbbfs_server_submit": (I, [P, i32, i32, P, P]),
@@ -489,6 +491,14 @@ def msbfs_device(g, sources, depth_bytes=1):
     _check(lib().gbbfs_msbfs_device(g.handle, _p(src), len(src), int(depth_bytes),
                                     ctypes.byref(ptr), ctypes.byref(st)), "msbfs_device")
     return ptr.value, st
+
+
+def msbfs_order(g, sources):
+    """Indices of `sources` in the order to batch them (gbbfs_msbfs_order)."""
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    order = np.empty(len(src), np.int32)
+    _check(lib().gbbfs_msbfs_order(g.handle, _p(src), len(src), _p(order)), "msbfs_order")
+    return order
 
 
 def msbfs_set_config(g, lanes=128, batch=8, alpha=15):

@@ -5,8 +5,9 @@
 Builds the reference's synthetic graph (-g/-u <scale>, -k <degree>; edge
 list from the host generator, CSR built on the GPU), picks -n sources with
 the reference's SourcePicker, runs them in batches of --lanes sources
-through gbbfs_msbfs_device and prints each batch's device time and phase
-shares, optionally its per-level times, and the queries/s of all batches.
+through gbbfs_msbfs_device (in gbbfs_msbfs_order's order unless
+--given-order) and prints each batch's device time and phase shares,
+optionally its per-level times, and the queries/s of all batches.
 """
 import argparse
 import sys
@@ -21,16 +22,20 @@ def main(argv=None):
     kind.add_argument("-u", type=int, help="uniform random graph of 2^scale vertices")
     ap.add_argument("-k", type=int, default=16, help="average degree")
     ap.add_argument("-n", type=int, default=256, help="sources")
-    ap.add_argument("--lanes", type=int, default=128, choices=(32, 64, 128))
+    ap.add_argument("--lanes", type=int, default=128, choices=(32, 64, 128, 256))
     ap.add_argument("--batch", type=int, default=8, choices=(4, 8, 16))
     ap.add_argument("--alpha", type=int, default=15)
     ap.add_argument("--depth-bytes", type=int, default=1, choices=(1, 4))
     ap.add_argument("--levels", action="store_true", help="print per-level times")
+    ap.add_argument("--given-order", action="store_true",
+                    help="batch the sources in SourcePicker order")
     a = ap.parse_args(argv)
     scale, uniform = (a.g, False) if a.g is not None else (a.u, True)
     with gbbfs.Graph.from_edges(gbbfs.generate_edges(scale, a.k, uniform)) as g:
         print("Graph has %d nodes and %d undirected edges" % (g.n, g.m // 2))
         srcs = gbbfs.pick_sources(g.offsets, a.n)
+        if not a.given_order:
+            srcs = srcs[gbbfs.msbfs_order(g, srcs)]
         gbbfs.msbfs_set_config(g, a.lanes, a.batch, a.alpha)
         total_ms = 0.0
         for b in range(0, a.n, a.lanes):

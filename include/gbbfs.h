@@ -184,13 +184,13 @@ int gbbfs_bc_bfs(gbbfs_graph* g, int32_t source, uint64_t* path_counts, int32_t*
 int gbbfs_bc(gbbfs_graph* g, const int32_t* sources, int64_t k, float* scores_out);
 
 /* ---- Batched multi-source BFS (no reference counterpart) ----
- * Many sources of one graph at once, 32, 64 or 128 per batch as a bitmask per
+ * Many sources of one graph at once, 32, 64, 128 or 256 per batch as a bitmask per
  * vertex, in one persistent kernel per batch captured in a CUDA graph.  Its
  * results are defined by the single-source search above: depth[s][v] equals
  * the depth gbbfs_bfs (and the reference's DOBFS, src/bfs.cc:142-188) gives v
  * from sources[s]. */
 typedef struct gbbfs_ms_config {
-  int32_t lanes;  /* sources per batch: 32, 64 or 128                    */
+  int32_t lanes;  /* sources per batch: 32, 64, 128 or 256               */
   int32_t batch;  /* neighbours one thread reads per bottom-up round: 4, 8, 16 */
   int32_t alpha;  /* a level runs top-down while its frontier's summed degree
                      is <= m_dir / alpha, bottom-up above                 */
@@ -220,7 +220,9 @@ typedef struct gbbfs_ms_stats {
  * row s for sources[s]: depth_bytes == 1 gives uint8 with 255 = unreached
  * (GBBFS_ERR_ARG if a depth exceeds 254), depth_bytes == 4 gives int32 with
  * -1 = unreached.  Batches run back to back; the copy of one batch overlaps
- * the next batch's search (pinned depth_out makes the copy asynchronous). */
+ * the next batch's search (pinned depth_out makes the copy asynchronous).
+ * More sources than one batch holds are batched in gbbfs_msbfs_order's
+ * order; rows still land at their sources' positions. */
 int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
                 void* depth_out, gbbfs_ms_stats* st);
 
@@ -228,6 +230,16 @@ int gbbfs_msbfs(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_byt
  * its k x n rows (valid until the next batched call on the handle). */
 int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int depth_bytes,
                        const void** depth_dev, gbbfs_ms_stats* st);
+
+/* The order to batch sources[0..k) in: order_out[j] (k entries) is the index
+ * of the j-th source to run.  A batch costs about as many full bottom-up
+ * levels as its slowest source needs, so sources that reach the bulk of the
+ * graph at the same level are put together: sorted (stably) by BFS depth
+ * from the highest-degree vertex (lowest id among ties), then by degree,
+ * highest first (degrees above 255 tie).  The first call on a handle runs
+ * that one search (replacing the handle's last single-source result) and
+ * keeps two bytes per vertex on the host. */
+int gbbfs_msbfs_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order_out);
 
 /* HBM (bytes) the batched search state of a graph with n vertices and m_dir
  * directed edges takes: the figure the query server admits graphs against. */
@@ -238,7 +250,7 @@ int gbbfs_msbfs_set_config(gbbfs_graph* g, const gbbfs_ms_config* cfg);
 int gbbfs_msbfs_get_config(const gbbfs_graph* g, gbbfs_ms_config* cfg);
 
 /* Autotuner: time every configuration of the built-in grid (lanes x batch x
- * alpha) on the given sample sources (up to 384 of them, in whole batches
+ * alpha) on the given sample sources (up to 512 of them, in whole batches
  * of each width), keep the fastest per query on the handle and return it in
  * *best. */
 int gbbfs_msbfs_autotune(gbbfs_graph* g, const int32_t* sample, int64_t k, int depth_bytes,

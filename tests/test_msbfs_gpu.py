@@ -18,7 +18,8 @@ def as_int32(d):
 
 @pytest.mark.parametrize("lanes,batch,alpha", [(64, 8, 15), (32, 4, 2), (64, 16, 200),
                                                (32, 8, 6), (64, 4, 1), (128, 8, 15),
-                                               (128, 4, 2), (128, 16, 200)])
+                                               (128, 4, 2), (128, 16, 200), (256, 8, 15),
+                                               (256, 4, 2), (256, 16, 200)])
 def test_msbfs_matches_single_source(native, lanes, batch, alpha):
     off, nbr = native.make_graph(16, 16, False)
     with native.Graph(off, nbr) as g:
@@ -34,12 +35,13 @@ def test_msbfs_matches_single_source(native, lanes, batch, alpha):
 
 
 @pytest.mark.parametrize("scale,uniform,lanes", [(15, True, 64), (18, False, 64),
-                                                 (15, True, 128), (18, False, 128)])
+                                                 (15, True, 128), (18, False, 128),
+                                                 (15, True, 256), (18, False, 256)])
 def test_msbfs_graphs(native, scale, uniform, lanes):
     off, nbr = native.make_graph(scale, 16, uniform)
     with native.Graph(off, nbr) as g:
         native.msbfs_set_config(g, lanes, 8, 15)
-        srcs = native.pick_sources(off, 200)
+        srcs = native.pick_sources(off, 300)
         ref = single_depths(native, g, srcs)
         assert np.array_equal(native.msbfs(g, srcs, 4), ref)
         # fewer sources than lanes, duplicate sources, any order
@@ -65,7 +67,7 @@ def test_msbfs_handmade(native):
 
 
 @pytest.mark.parametrize("alpha,lanes", [(1, 64), (15, 64), (100000, 64), (1, 128),
-                                         (100000, 128)])
+                                         (100000, 128), (1, 256), (100000, 256)])
 def test_msbfs_hubs(native, alpha, lanes):
     """Vertices above the hub degree are cut into work chunks in both directions."""
     rng = np.random.default_rng(3)
@@ -89,7 +91,7 @@ def test_msbfs_device_and_autotune(native):
     with native.Graph(off, nbr) as g:
         srcs = native.pick_sources(off, 64)
         best = native.msbfs_autotune(g, srcs, 1)
-        assert best["lanes"] in (32, 64, 128) and best["batch"] in (4, 8, 16)
+        assert best["lanes"] in (32, 64, 128, 256) and best["batch"] in (4, 8, 16)
         assert native.msbfs_get_config(g) == best
         ref = single_depths(native, g, srcs)
         assert np.array_equal(as_int32(native.msbfs(g, srcs, 1)), ref)
@@ -104,3 +106,29 @@ def test_msbfs_cli(native, capsys):
     assert msbfs_cli.main(["-g", "12", "-n", "40", "--lanes", "32", "--levels"]) == 0
     out = capsys.readouterr().out
     assert out.count("batch ") == 2 and "queries/s" in out and "level  1" in out
+    assert msbfs_cli.main(["-g", "12", "-n", "300", "--lanes", "256"]) == 0
+    out = capsys.readouterr().out
+    assert out.count("batch ") == 2 and "batch 1: 44 sources" in out
+
+
+def test_msbfs_order(native):
+    """Batching order: stable sort by (depth from the highest-degree vertex,
+    degree highest first, degrees above 255 tied)."""
+    off, nbr = native.make_graph(15, 16, False)
+    with native.Graph(off, nbr) as g:
+        deg = np.diff(off)
+        hub = int(np.argmax(deg))                    # lowest id among the maxima
+        hd = native.DOBFS(g, hub, depth=True)[1]
+        hd = np.where(hd < 0, 255, np.minimum(hd, 254)).astype(np.int64)
+        key = (hd << 8) | (255 - np.minimum(deg, 255))
+        srcs = native.pick_sources(off, 500)
+        srcs = np.concatenate([srcs, srcs[:7]])      # repeats keep their order
+        order = native.msbfs_order(g, srcs)
+        assert np.array_equal(order, np.argsort(key[srcs], kind="stable"))
+        assert len(native.msbfs_order(g, srcs[:0])) == 0
+        with pytest.raises(native.GbbfsError):
+            native.msbfs_order(g, [0, len(off) + 3])
+        # rows of a multi-batch call land at the callers' positions
+        native.msbfs_set_config(g, 32, 8, 15)
+        ref = single_depths(native, g, srcs[:80])
+        assert np.array_equal(native.msbfs(g, srcs[:80], 4), ref)
