@@ -484,7 +484,7 @@ def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
                 "td_ms": td_ms, "bu_ms": bu_ms, "rows_checked": 4}
 
 
-def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=2048):
+def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=4096):
     """Query server over the 8-graph pool: saturation throughput batched vs
     plain per-query launches, and p50/p99 latency under Poisson arrivals."""
     from dist_mem_gapbs_gb300 import serving
@@ -499,8 +499,11 @@ def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=2048):
     build_s = time.time() - t0
     out = {"pool": ["%s%d" % ("u" if u else "g", s) for s, u in pool], "build_s": build_s}
     try:
-        for mode, name in ((gbbfs.Server.BATCHED, "batched"), (gbbfs.Server.PLAIN, "plain")):
-            with gbbfs.Server(mode=mode) as srv:
+        for mode, order, name in ((gbbfs.Server.BATCHED, gbbfs.Server.GROUPED, "batched"),
+                                  (gbbfs.Server.BATCHED, gbbfs.Server.ARRIVAL,
+                                   "batched_arrival_order"),
+                                  (gbbfs.Server.PLAIN, gbbfs.Server.ARRIVAL, "plain")):
+            with gbbfs.Server(mode=mode, order=order) as srv:
                 for g in graphs:
                     srv.add_graph(g)
                 # warm every graph once
@@ -520,7 +523,7 @@ def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=2048):
                 res = srv.poll(burst + 16)
                 span = max(r["done_s"] for r in res) - t_start
                 out[name + "_saturation_qps"] = burst / span
-                if mode == gbbfs.Server.BATCHED:
+                if name == "batched":
                     out["latency"] = []
                     for rate in rates:
                         r = serving.run_open_loop(srv, sources, rate, duration_s)

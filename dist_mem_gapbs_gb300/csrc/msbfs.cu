@@ -33,7 +33,7 @@ constexpr int kSrcSlot = kMsMaxLanes + 1;   // per batch buffer: count, then the
 constexpr int kLaneClasses = 4;              // lane words of 32 << cls bits
 
 struct MsConfig {
-  int lanes = 128;       // 32, 64, 128 or 256 sources per batch (the widest used)
+  int lanes = 256;       // 32, 64, 128 or 256 sources per batch (the widest used)
   int batch = 8;         // neighbours per bottom-up round of one thread
   int alpha = 15;        // top-down while frontier degrees <= m / alpha
 };

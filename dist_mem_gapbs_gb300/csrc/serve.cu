@@ -5,7 +5,9 @@
 // pending queries of each graph into the lanes of the multi-source search:
 // whenever one of a graph's two batch buffers is free, up to `lanes` queued
 // queries of that graph are launched together, so queries that arrive while
-// a batch is on the GPU join the next one.  Batches of different graphs run
+// a batch is on the GPU join the next one.  When more are queued than one
+// batch holds, the batch is formed from queries whose sources have close
+// batching keys (gbbfs_msbfs_order), around the oldest query.  Batches of different graphs run
 // on their graphs' own streams and overlap on the device.  The per-graph
 // search state (visit / frontier words, depth rows) is admitted against free
 // HBM and an optional byte budget; an idle graph gives its state back when
@@ -26,6 +28,7 @@
 #include <cstring>
 #include <deque>
 #include <mutex>
+#include <numeric>
 #include <thread>
 #include <vector>
 
@@ -154,6 +157,8 @@ bool admit(gbbfs_server* s, size_t idx) {
                            state_bytes_in_use(s) + need <= s->cfg.hbm_budget_bytes;
     if (hbm_ok && budget_ok) {
       if (ms_prepare(sl.g, 1) != GBBFS_OK) return false;
+      // Batching keys, once per graph (k = 0: keys only).
+      if (s->cfg.order == 0 && ms_order(sl.g, nullptr, 0, nullptr) != GBBFS_OK) return false;
       sl.admitted = true;
       return true;
     }
@@ -218,21 +223,66 @@ void harvest(gbbfs_server* s, Slot& sl) {
   }
 }
 
+constexpr size_t kGroupWindow = 4;   // batches' worth of the oldest queries a batch is chosen from
+
+// The queries of a slot's next batch (at most `lanes`): all of them when they
+// fit, or in arrival order when grouping is off.  Otherwise the oldest
+// kGroupWindow * lanes pending queries are sorted (stably) by their sources'
+// batching keys, and the batch is the run of `lanes` consecutive ones in that
+// order with the smallest key spread among the runs that hold the oldest
+// query.  The oldest query always goes, so a query waits for at most as many
+// launches of its graph as there are queries ahead of it.
+void take_batch(gbbfs_server* s, Slot& sl, size_t lanes, std::vector<Query>& out) {
+  const size_t P = sl.pending.size();
+  const std::vector<uint16_t>& keys = sl.g->batch_key;
+  if (P <= lanes || s->cfg.order != 0 || keys.size() != (size_t)sl.g->n) {
+    const size_t k = std::min(P, lanes);
+    for (size_t i = 0; i < k; i++) {
+      out.push_back(sl.pending.front());
+      sl.pending.pop_front();
+    }
+    return;
+  }
+  const size_t W = std::min(P, kGroupWindow * lanes);
+  auto key = [&](uint32_t i) { return (int)keys[(size_t)sl.pending[i].source]; };
+  std::vector<uint32_t> idx(W);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return key(a) < key(b); });
+  const size_t p = (size_t)(std::find(idx.begin(), idx.end(), 0u) - idx.begin());
+  const size_t lo = p + 1 >= lanes ? p + 1 - lanes : 0;
+  const size_t hi = std::min(p, W - lanes);
+  size_t best = lo;
+  int best_spread = key(idx[lo + lanes - 1]) - key(idx[lo]);
+  for (size_t st = lo + 1; st <= hi; st++) {
+    const int spread = key(idx[st + lanes - 1]) - key(idx[st]);
+    if (spread < best_spread) {
+      best_spread = spread;
+      best = st;
+    }
+  }
+  std::vector<char> take(W, 0);
+  for (size_t j = best; j < best + lanes; j++) take[idx[j]] = 1;
+  std::vector<Query> rest;
+  rest.reserve(W - lanes);
+  for (size_t i = 0; i < W; i++) (take[i] ? out : rest).push_back(sl.pending[i]);
+  sl.pending.erase(sl.pending.begin(), sl.pending.begin() + (std::ptrdiff_t)W);
+  sl.pending.insert(sl.pending.begin(), rest.begin(), rest.end());
+}
+
 // Launch the next batch of a slot into a free buffer.
 void launch(gbbfs_server* s, Slot& sl) {
   for (int b = 0; b < 2 && !sl.pending.empty(); b++) {
     Inflight& f = sl.fl[b];
     if (f.busy) continue;
     const int lanes = std::min<int>(ms_lanes(sl.g), std::max(1, s->cfg.max_batch));
-    const int k = (int)std::min<size_t>(sl.pending.size(), (size_t)lanes);
+    take_batch(s, sl, (size_t)lanes, f.q);
+    const int k = (int)f.q.size();
     std::vector<int32_t> src(k);
     const double t = s->now();
     for (int i = 0; i < k; i++) {
-      f.q.push_back(sl.pending.front());
-      sl.pending.pop_front();
-      f.q.back().t_start = t;
-      f.q.back().batch = k;
-      src[i] = f.q.back().source;
+      f.q[i].t_start = t;
+      f.q[i].batch = k;
+      src[i] = f.q[i].source;
     }
     int st = ms_launch(sl.g, b, src.data(), k);
     if (st == GBBFS_OK) {
@@ -351,12 +401,12 @@ int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out) {
   gbbfs_server* s = new (std::nothrow) gbbfs_server();
   if (!s) return GBBFS_ERR_NOMEM;
   memset(&s->cfg, 0, sizeof s->cfg);
-  s->cfg.max_batch = 128;
+  s->cfg.max_batch = kMsMaxLanes;
   if (cfg) s->cfg = *cfg;
-  if (s->cfg.max_batch <= 0) s->cfg.max_batch = 128;
-  if (s->cfg.mode != 0 && s->cfg.mode != 1) {
+  if (s->cfg.max_batch <= 0) s->cfg.max_batch = kMsMaxLanes;
+  if ((s->cfg.mode != 0 && s->cfg.mode != 1) || (s->cfg.order != 0 && s->cfg.order != 1)) {
     delete s;
-    last_error() = "server mode must be 0 (batched) or 1 (plain)";
+    last_error() = "server mode must be 0 (batched) or 1 (plain), order 0 (grouped) or 1 (arrival)";
     return GBBFS_ERR_ARG;
   }
   s->t0 = Clock::now();

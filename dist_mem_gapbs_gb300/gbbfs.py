@@ -501,7 +501,7 @@ def msbfs_order(g, sources):
     return order
 
 
-def msbfs_set_config(g, lanes=128, batch=8, alpha=15):
+def msbfs_set_config(g, lanes=256, batch=8, alpha=15):
     c = MsConfig(lanes, batch, alpha)
     _check(lib().gbbfs_msbfs_set_config(g.handle, ctypes.byref(c)), "msbfs_set_config")
 
@@ -534,7 +534,8 @@ def msbfs_autotune(g, sample, depth_bytes=1):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("max_batch", ctypes.c_int32),
-                ("hbm_budget_bytes", ctypes.c_int64), ("hbm_reserve_bytes", ctypes.c_int64)]
+                ("hbm_budget_bytes", ctypes.c_int64), ("hbm_reserve_bytes", ctypes.c_int64),
+                ("order", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -561,8 +562,11 @@ class Server:
     PLAIN = 1
     BATCHED = 0
 
-    def __init__(self, mode=0, max_batch=128, hbm_budget_bytes=0, hbm_reserve_bytes=0):
-        cfg = ServerConfig(mode, max_batch, hbm_budget_bytes, hbm_reserve_bytes)
+    GROUPED = 0
+    ARRIVAL = 1
+
+    def __init__(self, mode=0, max_batch=256, hbm_budget_bytes=0, hbm_reserve_bytes=0, order=0):
+        cfg = ServerConfig(mode, max_batch, hbm_budget_bytes, hbm_reserve_bytes, order, 0)
         h = ctypes.c_void_p()
         _check(lib().gbbfs_server_open(ctypes.byref(cfg), ctypes.byref(h)), "server_open")
         self._h = h

@@ -22,7 +22,7 @@ def main(argv=None):
     kind.add_argument("-u", type=int, help="uniform random graph of 2^scale vertices")
     ap.add_argument("-k", type=int, default=16, help="average degree")
     ap.add_argument("-n", type=int, default=256, help="sources")
-    ap.add_argument("--lanes", type=int, default=128, choices=(32, 64, 128, 256))
+    ap.add_argument("--lanes", type=int, default=256, choices=(32, 64, 128, 256))
     ap.add_argument("--batch", type=int, default=8, choices=(4, 8, 16))
     ap.add_argument("--alpha", type=int, default=15)
     ap.add_argument("--depth-bytes", type=int, default=1, choices=(1, 4))

@@ -272,9 +272,14 @@ typedef struct gbbfs_server gbbfs_server;
 
 typedef struct gbbfs_server_config {
   int32_t mode;              /* 0: batched multi-source; 1: one plain search per query */
-  int32_t max_batch;         /* queries per batch, <= lanes (default 128)        */
+  int32_t max_batch;         /* queries per batch, <= lanes (default 256)        */
   int64_t hbm_budget_bytes;  /* cap on per-graph search state, 0 = none          */
   int64_t hbm_reserve_bytes; /* free HBM to leave untouched                      */
+  int32_t order;             /* 0: when more queries of a graph wait than a batch
+                                holds, batch those with close batching keys
+                                (gbbfs_msbfs_order) around the oldest; 1: strict
+                                arrival order                                   */
+  int32_t pad;
 } gbbfs_server_config;
 
 typedef struct gbbfs_result {

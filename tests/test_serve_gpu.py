@@ -106,20 +106,67 @@ def test_admission_budget(native, pool):
             assert r["checksum"] == native.depth_checksum(exp[(r["graph_id"], r["source"])])
 
 
-def test_full_width_batches(native, pool):
-    """More queries on one graph than two batches of the widest lane word
-    hold: both batch buffers run full 128-query batches, every digest exact."""
+@pytest.mark.parametrize("max_batch,order", [(256, 0), (128, 1), (128, 0)])
+def test_full_width_batches(native, pool, max_batch, order):
+    """More queries on one graph than two batches hold: both batch buffers run
+    full batches (256 lanes: the widest word), every digest exact."""
     off, g = pool[2]
     srcs = [int(s) for s in native.pick_sources(off, 40)]
     exp = {s: u8(native.DOBFS(g, s, depth=True)[1]) for s in srcs}
-    keys = [(0, srcs[i % len(srcs)]) for i in range(400)]
-    with native.Server(mode=0) as srv:
+    keys = [(0, srcs[i % len(srcs)]) for i in range(2 * max_batch + 150)]
+    with native.Server(mode=0, max_batch=max_batch, order=order) as srv:
         srv.add_graph(g)
         res, _ = run_queries(native, srv, keys, [g.n], False)
-        assert max(r["batch_size"] for r in res) == 128
+        assert max(r["batch_size"] for r in res) == max_batch
         for r in res:
             assert r["status"] == 0
             assert r["checksum"] == native.depth_checksum(exp[r["source"]])
+
+
+def batch_key(native, off, g):
+    deg = np.diff(off)
+    hd = native.DOBFS(g, int(np.argmax(deg)), depth=True)[1]
+    hd = np.where(hd < 0, 255, np.minimum(hd, 254)).astype(np.int64)
+    return (hd << 8) | (255 - np.minimum(deg, 255))
+
+
+def test_grouped_batches(native, pool):
+    """With more queries waiting than a batch holds, grouped batches hold
+    sources of closer batching keys than arrival-order batches, the oldest
+    query goes in the first batch, and every digest is exact."""
+    off, g = pool[0]
+    key = batch_key(native, off, g)
+    srcs = [int(s) for s in native.pick_sources(off, 40)]
+    exp = {s: u8(native.DOBFS(g, s, depth=True)[1]) for s in srcs}
+    rng = np.random.default_rng(5)
+    keys = [(0, srcs[i]) for i in rng.integers(len(srcs), size=600)]
+    spread = {}
+    for order in (0, 1):
+        with native.Server(mode=0, max_batch=32, order=order) as srv:
+            srv.add_graph(g)
+            srv.submit(0, srcs[0])          # admission (and the batching keys) first
+            srv.drain()
+            srv.poll(16)
+            tickets = srv.submit_many([k[0] for k in keys], [k[1] for k in keys])
+            srv.drain()
+            res = []
+            while True:
+                got = srv.poll(4096)
+                if not got:
+                    break
+                res += got
+            assert len(res) == len(keys)
+            for r in res:
+                assert r["status"] == 0
+                assert r["checksum"] == native.depth_checksum(exp[r["source"]])
+            first = min(res, key=lambda r: r["ticket"])
+            assert first["ticket"] == tickets[0]
+            assert first["start_s"] == min(r["start_s"] for r in res)
+            batches = {}
+            for r in res:
+                batches.setdefault(r["start_s"], []).append(key[r["source"]])
+            spread[order] = np.mean([max(b) - min(b) for b in batches.values()])
+    assert spread[0] < spread[1]
 
 
 def test_submit_many(native, pool):
