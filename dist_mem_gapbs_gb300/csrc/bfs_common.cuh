@@ -52,6 +52,7 @@ struct DevStep {
 struct DevState {
   int32_t source, alpha, beta, want_depth;
   int32_t instrument, in_graph, pad0, pad1;
+  int32_t* parent;    // this search's parent array (32 W entries)
   // DOBFS control (src/bfs.cc:158-185): the reference's int64 counters.
   int64_t edges_to_check, scout, cur_edges, awake, old_awake, visited, F;
   int64_t iter, max_iter;
@@ -75,7 +76,6 @@ struct Bufs {
   uint32_t* visited;
   uint32_t* bm0;
   uint32_t* bm1;
-  int32_t* parent;
   int32_t* depth;
   int32_t* qv0;
   int32_t* qv1;

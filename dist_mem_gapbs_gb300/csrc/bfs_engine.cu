@@ -113,7 +113,6 @@ Bufs<OffT> bufs(const gbbfs_graph* g) {
   b.visited = g->visited;
   b.bm0 = g->bm[0];
   b.bm1 = g->bm[1];
-  b.parent = g->parent;
   b.depth = g->depth;
   b.qv0 = g->qv[0];
   b.qv1 = g->qv[1];
@@ -397,8 +396,10 @@ int64_t alg_bytes(int64_t n, const gbbfs_step* steps, int count) {
   return b;
 }
 
+// One search into parent_buf (32 W entries; the handle's own array when
+// null).
 int search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
-           gbbfs_stats* st) {
+           gbbfs_stats* st, int32_t* parent_buf = nullptr) {
   if (!g) return GBBFS_ERR_ARG;
   if (source < 0 || source >= g->n) {
     g_last_error = "source out of range";
@@ -415,6 +416,7 @@ int search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
   h->alpha = alpha;
   h->beta = beta;
   h->want_depth = want_depth ? 1 : 0;
+  h->parent = parent_buf ? parent_buf : g->parent;
   h->instrument = instrument ? 1 : 0;
   h->in_graph = stepped ? 0 : 1;
   std::vector<double> kernel_seconds;
@@ -431,6 +433,7 @@ int search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
   }
   g->have_result = true;
   g->result_depth = want_depth;
+  g->last_parent = parent_buf ? parent_buf : g->parent;
   if (st) {
     float ms = 0;
     GB_CUDA(cudaEventElapsedTime(&ms, g->ev_begin, g->ev_end));
@@ -549,7 +552,7 @@ int gbbfs_results(gbbfs_graph* g, int32_t* parent_out, int32_t* depth_out) {
   if (!g->have_result || (depth_out && !g->result_depth)) return GBBFS_ERR_STATE;
   GB_CUDA(cudaSetDevice(g->device));
   if (parent_out)
-    GB_CUDA(cudaMemcpyAsync(parent_out, g->parent, sizeof(int32_t) * g->n,
+    GB_CUDA(cudaMemcpyAsync(parent_out, g->last_parent, sizeof(int32_t) * g->n,
                             cudaMemcpyDeviceToHost, g->stream));
   if (depth_out)
     GB_CUDA(cudaMemcpyAsync(depth_out, g->depth, sizeof(int32_t) * g->n,
@@ -561,7 +564,7 @@ int gbbfs_results(gbbfs_graph* g, int32_t* parent_out, int32_t* depth_out) {
 int gbbfs_result_device_ptrs(gbbfs_graph* g, const int32_t** parent, const int32_t** depth) {
   if (!g) return GBBFS_ERR_ARG;
   if (!g->have_result) return GBBFS_ERR_STATE;
-  if (parent) *parent = g->parent;
+  if (parent) *parent = g->last_parent;
   if (depth) *depth = g->result_depth ? g->depth : nullptr;
   return GBBFS_OK;
 }
@@ -581,12 +584,12 @@ int gbbfs_bfs_many(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha,
   GB_CUDA(cudaSetDevice(g->device));
   if (!g->copy_stream) {
     for (int i = 0; i < 2; i++) {
-      cudaError_t e = cudaMalloc(&g->stage[i], sizeof(int32_t) * (size_t)g->n);
+      cudaError_t e = cudaMalloc(&g->stage[i], sizeof(int32_t) * 32 * (size_t)g->W);
       if (e != cudaSuccess) {
-        g_last_error = std::string("staging arrays: ") + cudaGetErrorString(e);
+        g_last_error = std::string("parent arrays: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? GBBFS_ERR_NOMEM : GBBFS_ERR_CUDA;
       }
-      g->device_bytes += (int64_t)sizeof(int32_t) * g->n;
+      g->device_bytes += (int64_t)sizeof(int32_t) * 32 * g->W;
       GB_CUDA(cudaEventCreateWithFlags(&g->staged[i], cudaEventDisableTiming));
       GB_CUDA(cudaEventCreateWithFlags(&g->copied[i], cudaEventDisableTiming));
     }
@@ -596,11 +599,11 @@ int gbbfs_bfs_many(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha,
   int rc = GBBFS_OK;
   for (int64_t i = 0; i < k && rc == GBBFS_OK; i++) {
     const int b = (int)(i & 1);
-    // staging array b is free once the copy of search i-2 has left it
+    // Search i writes parent array b, which is free once the copy of search
+    // i-2 has left it; its copy to the host then runs beside search i+1.
     GB_CUDA(cudaStreamWaitEvent(g->stream, g->copied[b], 0));
-    rc = search(g, sources[i], alpha, beta, false, st ? st + i : nullptr);
+    rc = search(g, sources[i], alpha, beta, false, st ? st + i : nullptr, g->stage[b]);
     if (rc != GBBFS_OK) break;
-    GB_CUDA(cudaMemcpyAsync(g->stage[b], g->parent, bytes, cudaMemcpyDeviceToDevice, g->stream));
     GB_CUDA(cudaEventRecord(g->staged[b], g->stream));
     GB_CUDA(cudaStreamWaitEvent(g->copy_stream, g->staged[b], 0));
     GB_CUDA(cudaMemcpyAsync(parent_out[i], g->stage[b], bytes, cudaMemcpyDeviceToHost,

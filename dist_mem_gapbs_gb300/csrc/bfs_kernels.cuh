@@ -6,7 +6,8 @@
 //   iso      u32[W]      bit set for degree-0 vertices and ids >= n
 //   visited  u32[W]      bit set once a vertex has a parent
 //   bm0/bm1  u32[W]      bottom-up frontier and the one being built (swap by parity)
-//   parent   int32[32W]  the BFS tree, -1 while unvisited
+//   parent   int32[32W]  the BFS tree, -1 while unvisited (the array the
+//                        search's parameters name: the caller may alternate)
 //   depth    int32[32W]  BFS depth, -1 while unvisited (kept on request)
 //   qv/qs    frontier queues: vertex ids and the exclusive prefix sum of their
 //            out-degrees, in queue order (two of each, current and next)
@@ -37,6 +38,7 @@ __global__ void __launch_bounds__(kThreads) k_init(Bufs<OffT> b) {
   DevState* st = b.st;
   stamp_begin(st);
   const int32_t source = st->source;
+  int32_t* parent = st->parent;
   int32_t* depth = st->want_depth ? b.depth : nullptr;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -55,8 +57,8 @@ __global__ void __launch_bounds__(kThreads) k_init(Bufs<OffT> b) {
   for (int64_t i = tid; i < nvec; i += stride) {
     const bool here = i == src_vec;
     const int la = here ? src_lane : -1, lb = here ? src_lane - 4 : -1;
-    reinterpret_cast<int4*>(b.parent)[2 * i] = put(neg, la, source);
-    reinterpret_cast<int4*>(b.parent)[2 * i + 1] = put(neg, lb, source);
+    reinterpret_cast<int4*>(parent)[2 * i] = put(neg, la, source);
+    reinterpret_cast<int4*>(parent)[2 * i + 1] = put(neg, lb, source);
     if (depth) {
       reinterpret_cast<int4*>(depth)[2 * i] = put(neg, la, 0);
       reinterpret_cast<int4*>(depth)[2 * i + 1] = put(neg, lb, 0);
@@ -239,6 +241,7 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
   stamp_begin(st);
   const int cur = st->cur;
   const int level = st->level;
+  int32_t* parent = st->parent;
   int32_t* depth = st->want_depth ? b.depth : nullptr;
   const int32_t* qv = cur ? b.qv1 : b.qv0;
   const OffT* qs = cur ? b.qs1 : b.qs0;
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
 #pragma unroll
         for (int q = 0; q < kHub; q++) {
           if (cl[q]) {
-            b.parent[v[q]] = u;
+            parent[v[q]] = u;
             if (depth) depth[v[q]] = level;
           }
           stage(cl[q], v[q]);
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
           const uint32_t old = atomicOr(wp, bit);
           if (!(old & bit)) {
             claimed = true;
-            b.parent[v] = u;
+            parent[v] = u;
             if (depth) depth[v] = level;
           }
         }
@@ -476,7 +479,7 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
   const OffT* __restrict__ off = b.off;
   const int32_t* __restrict__ nbr = b.nbr;
   uint32_t* __restrict__ visited = b.visited;
-  int32_t* __restrict__ parent = b.parent;
+  int32_t* __restrict__ parent = st->parent;
   const int64_t W = b.W;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;

@@ -86,6 +86,7 @@ struct gbbfs_graph {
   uint32_t* visited = nullptr;
   uint32_t* bm[2] = {nullptr, nullptr};
   int32_t* parent = nullptr;
+  int32_t* last_parent = nullptr;   // parent array of the last search
   int32_t* depth = nullptr;
   int32_t* qv[2] = {nullptr, nullptr};
   void* qs[2] = {nullptr, nullptr};
@@ -106,7 +107,8 @@ struct gbbfs_graph {
   // Batching key per vertex (host): BFS depth from the highest-degree vertex
   // (255 = unreached) << 8 | (255 - min(degree, 255)).  Made on first use.
   std::vector<uint16_t> batch_key;
-  // gbbfs_bfs_many: staged parent arrays and their copy-out stream.
+  // gbbfs_bfs_many: the two parent arrays its searches alternate between,
+  // and the stream that copies them out.
   int32_t* stage[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t staged[2] = {nullptr, nullptr};

@@ -142,7 +142,7 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   b.visited = reinterpret_cast<uint32_t*>(base + kOffVisited);
   b.bm0 = reinterpret_cast<uint32_t*>(base + kOffBm0);
   b.bm1 = reinterpret_cast<uint32_t*>(base + kOffBm1);
-  b.parent = reinterpret_cast<int32_t*>(base + kOffParent);
+  int32_t* parent = reinterpret_cast<int32_t*>(base + kOffParent);
   b.depth = reinterpret_cast<int32_t*>(base + kOffDepth);
   b.qv0 = reinterpret_cast<int32_t*>(base + kOffQv0);
   b.qv1 = reinterpret_cast<int32_t*>(base + kOffQv1);
@@ -170,6 +170,7 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   head.alpha = alpha;
   head.beta = beta;
   head.want_depth = d_depth_out ? 1 : 0;
+  head.parent = parent;
   head.instrument = 0;
   head.in_graph = 0;
   head.t0 = ~0ull;
@@ -210,7 +211,7 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   }
   int32_t err = 0;
   GB_CUDA(cudaMemcpyAsync(&err, &b.st->error, sizeof err, cudaMemcpyDeviceToHost, s));
-  GB_CUDA(cudaMemcpyAsync(d_parent_out, b.parent, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice,
+  GB_CUDA(cudaMemcpyAsync(d_parent_out, parent, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice,
                           s));
   if (d_depth_out)
     GB_CUDA(cudaMemcpyAsync(d_depth_out, b.depth, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice,

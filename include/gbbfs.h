@@ -116,11 +116,11 @@ int gbbfs_bfs(gbbfs_graph* g, int32_t source, int alpha, int beta,
 /* The benchmark's trial loop over sources (src/benchmark.h:126-131, one
  * DOBFS per trial) as one call: searches from sources[0..k) run back to
  * back, and search i's parent array goes to parent_out[i] (host, n entries;
- * pinned memory makes the copy asynchronous).  Each result is staged in HBM
- * and copied out on a second stream while the next search runs.  Pointers
- * may repeat: copies land in source order, so the last one wins.  st may be
- * NULL or hold k entries.  Allocates two n-entry staging arrays on first
- * use. */
+ * pinned memory makes the copy asynchronous).  The searches alternate
+ * between two parent arrays in HBM, and each is copied out on a second
+ * stream while the next search runs.  Pointers may repeat: copies land in
+ * source order, so the last one wins.  st may be NULL or hold k entries.
+ * Allocates those two parent arrays on first use. */
 int gbbfs_bfs_many(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha, int beta,
                    int32_t* const* parent_out, gbbfs_stats* st);
 
