@@ -68,6 +68,7 @@ void release(gbbfs_graph* g) {
     if (g->copied[i]) cudaEventDestroy(g->copied[i]);
   }
   if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
+  if (g->h_slot) cudaFreeHost(g->h_slot);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->off);
@@ -311,6 +312,56 @@ int run_graph(gbbfs_graph* g) {
   GB_CUDA(cudaGraphLaunch(g->exec, g->stream));
   GB_CUDA(cudaEventRecord(g->ev_end, g->stream));
   GB_CUDA(cudaEventSynchronize(g->ev_end));
+  return GBBFS_OK;
+}
+
+// The trial loop's searches without stats: search i reads its parameters
+// from host slot i & 1 and reads its header back into the same slot, so the
+// host queues search i while search i-1 still runs and only waits for search
+// i-2 (the last user of the slot).  The graph's own read-back into h_st
+// still happens and is not used here.
+template <typename OffT>
+int run_many_graph(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha, int beta,
+                   int32_t* const* parent_out) {
+  if (!g->exec) GB_TRY(build_graph<OffT>(g));
+  const size_t bytes = sizeof(int32_t) * (size_t)g->n;
+  const size_t header = offsetof(DevState, trace);
+  auto finish = [&](int64_t i) -> int {
+    const int b = (int)(i & 1);
+    GB_CUDA(cudaEventSynchronize(g->staged[b]));
+    if (g->h_slot[b].error) {
+      g_last_error = "device control loop exceeded its iteration bound";
+      return g->h_slot[b].error;
+    }
+    return GBBFS_OK;
+  };
+  for (int64_t i = 0; i < k; i++) {
+    const int b = (int)(i & 1);
+    if (i >= 2) GB_TRY(finish(i - 2));
+    DevState* h = g->h_slot + b;
+    memset(h, 0, header);
+    h->source = sources[i];
+    h->alpha = alpha;
+    h->beta = beta;
+    h->in_graph = 1;
+    h->parent = g->stage[b];
+    // Parent array b is free once the copy of search i-2 has left it.
+    GB_CUDA(cudaStreamWaitEvent(g->stream, g->copied[b], 0));
+    GB_CUDA(cudaMemcpyAsync(g->st, h, kParamBytes, cudaMemcpyHostToDevice, g->stream));
+    GB_CUDA(cudaGraphLaunch(g->exec, g->stream));
+    GB_CUDA(cudaMemcpyAsync(h, g->st, header, cudaMemcpyDeviceToHost, g->stream));
+    GB_CUDA(cudaEventRecord(g->staged[b], g->stream));
+    GB_CUDA(cudaStreamWaitEvent(g->copy_stream, g->staged[b], 0));
+    GB_CUDA(cudaMemcpyAsync(parent_out[i], g->stage[b], bytes, cudaMemcpyDeviceToHost,
+                            g->copy_stream));
+    GB_CUDA(cudaEventRecord(g->copied[b], g->copy_stream));
+  }
+  for (int64_t i = std::max<int64_t>(0, k - 2); i < k; i++) GB_TRY(finish(i));
+  if (k > 0) {
+    g->have_result = true;
+    g->result_depth = false;
+    g->last_parent = g->stage[(k - 1) & 1];
+  }
   return GBBFS_OK;
 }
 
@@ -594,6 +645,24 @@ int gbbfs_bfs_many(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha,
       GB_CUDA(cudaEventCreateWithFlags(&g->copied[i], cudaEventDisableTiming));
     }
     GB_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->h_slot), 2 * sizeof(DevState),
+                          cudaHostAllocDefault));
+  }
+  if (!st) {
+    if (alpha <= 0) alpha = 15;
+    if (beta <= 0) beta = 18;
+    for (int64_t i = 0; i < k; i++) {
+      if (sources[i] < 0 || sources[i] >= g->n) {
+        g_last_error = "source out of range";
+        return GBBFS_ERR_ARG;
+      }
+    }
+    g->have_result = false;
+    int rc = g->off32 ? run_many_graph<uint32_t>(g, sources, k, alpha, beta, parent_out)
+                      : run_many_graph<unsigned long long>(g, sources, k, alpha, beta, parent_out);
+    GB_CUDA(cudaStreamSynchronize(g->copy_stream));
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    return rc;
   }
   const size_t bytes = sizeof(int32_t) * (size_t)g->n;
   int rc = GBBFS_OK;

@@ -113,4 +113,7 @@ struct gbbfs_graph {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t staged[2] = {nullptr, nullptr};
   cudaEvent_t copied[2] = {nullptr, nullptr};
+  // Its searches without stats: parameters and read-back headers per slot
+  // (pinned), so a search is queued before the one before it has finished.
+  gbbfs::DevState* h_slot = nullptr;
 };

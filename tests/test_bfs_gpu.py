@@ -198,6 +198,12 @@ def test_many_searches_pipelined(native, oracle):
         native.bfs_many(g, srcs[::-1], one)
         ok, why = oracle.verify(off, nbr, int(srcs[0]), one)
         assert ok, why
+        last = np.empty(g.n, np.int32)
+        native.results(g, last, None)         # the handle's result: the last search
+        assert np.array_equal(last, one)
+        for i in range(2):                    # fewer searches than parent arrays
+            native.bfs_many(g, srcs[i:i + 1], one)
+            assert oracle.verify(off, nbr, int(srcs[i]), one)[0]
         native.bfs_many(g, srcs[:0], one)
         with pytest.raises(native.GbbfsError):
             native.bfs_many(g, np.array([srcs[0], g.n + 2], np.int32),
