@@ -521,6 +521,30 @@ int search(gbbfs_graph* g, int32_t source, int alpha, int beta, bool want_depth,
 
 namespace gbbfs {
 
+int bfs_enqueue(gbbfs_graph* g, int32_t source, void* h_params) {
+  if (source < 0 || source >= g->n) {
+    g_last_error = "source out of range";
+    return GBBFS_ERR_ARG;
+  }
+  if (!g->exec) GB_TRY(g->off32 ? build_graph<uint32_t>(g) : build_graph<unsigned long long>(g));
+  DevState* h = static_cast<DevState*>(h_params);   // only the parameter head is written
+  memset(h, 0, kParamBytes);
+  h->source = source;
+  h->alpha = 15;
+  h->beta = 18;
+  h->want_depth = 1;
+  h->in_graph = 1;
+  h->parent = g->parent;
+  GB_CUDA(cudaMemcpyAsync(g->st, h, kParamBytes, cudaMemcpyHostToDevice, g->stream));
+  GB_CUDA(cudaGraphLaunch(g->exec, g->stream));
+  g->have_result = false;   // queued searches leave no result on the handle
+  return GBBFS_OK;
+}
+
+const int32_t* bfs_depth(const gbbfs_graph* g) { return g->depth; }
+
+const int32_t* bfs_error_word(const gbbfs_graph* g) { return &g->st->error; }
+
 // A handle from a CSR already in device memory (offsets int64[n+1],
 // neighbours int32[m]); the arrays are copied, the caller keeps them.
 int graph_create_device(const int64_t* d_off, const int32_t* d_nbr, int64_t n, int64_t m,

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -42,6 +43,10 @@ int ms_finish(gbbfs_graph* g, int buf);            // wait, then report its stat
 void* ms_depth(gbbfs_graph* g, int buf);           // device rows of `buf`
 cudaEvent_t ms_done_event(gbbfs_graph* g, int buf);
 void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s);  // copies out of `buf` queued on s
+// Device time (ms) of the search kernel of the finished batch in `buf`, from
+// its own start and end stamps (a cooperative kernel runs alone once started,
+// so this excludes waits for other work).
+double ms_kernel_ms(const gbbfs_graph* g, int buf);
 // Indices of sources[0..k) in the order to batch them (gbbfs_msbfs_order).
 int ms_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order);
 
@@ -49,6 +54,18 @@ int ms_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order);
 // (gpu_build.cu); keys and tmp hold len each, *out is the sorted one.
 int radix_sort64(uint64_t* keys, uint64_t* tmp, int64_t len, int key_bits, cudaStream_t s,
                  uint64_t** out);
+
+// Single-source searches queued without waiting (bfs_engine.cu), for the
+// query server.  bfs_enqueue queues one search from `source` on the handle's
+// stream: its parameters come from the caller's pinned block of
+// kSearchParamBytes, which must stay untouched until the search has run;
+// depths are kept in bfs_depth(g) and parents in the handle's own array, and
+// bfs_error_word(g) (device) holds the search's error status.  The caller
+// orders its reads of them on the same stream, before the next search.
+constexpr size_t kSearchParamBytes = offsetof(DevState, edges_to_check);
+int bfs_enqueue(gbbfs_graph* g, int32_t source, void* h_params);
+const int32_t* bfs_depth(const gbbfs_graph* g);
+const int32_t* bfs_error_word(const gbbfs_graph* g);
 
 // A handle from a CSR in device memory (bfs_engine.cu): offsets int64[n+1]
 // and neighbours int32[m], copied into the handle.

@@ -763,6 +763,11 @@ int ms_finish(gbbfs_graph* g, int buf) {
 
 void* ms_depth(gbbfs_graph* g, int buf) { return g->ms->depth[buf]; }
 
+double ms_kernel_ms(const gbbfs_graph* g, int buf) {
+  const MsCtl& c = g->ms->h_ctl[buf];
+  return c.t_end > c.t_begin ? (double)(c.t_end - c.t_begin) * 1e-6 : 0.0;
+}
+
 cudaEvent_t ms_done_event(gbbfs_graph* g, int buf) { return g->ms->computed[buf]; }
 
 void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s) {

@@ -7,7 +7,16 @@
 // queries of that graph are launched together, so queries that arrive while
 // a batch is on the GPU join the next one.  When more are queued than one
 // batch holds, the batch is formed from queries whose sources have close
-// batching keys (gbbfs_msbfs_order), around the oldest query.  Batches of different graphs run
+// batching keys (gbbfs_msbfs_order), around the oldest query.  A launch of
+// few queries runs them as plain single-source searches instead when that
+// is cheaper: per graph the server measures a plain search's device time
+// when it admits the graph, keeps a running estimate of a batch's at each
+// lane width (the search kernel's own start and end stamps, which exclude
+// waits for other graphs' work; one 1-source batch is measured at
+// admission too), and picks plain when k plain searches are estimated to
+// take less than one batch and few batches are in flight: the small kernels
+// of a plain search queue behind other graphs' batches, which hold the whole
+// GPU, so under load a batch answers sooner.  Batches of different graphs run
 // on their graphs' own streams and overlap on the device.  The per-graph
 // search state (visit / frontier words, depth rows) is admitted against free
 // HBM and an optional byte budget; an idle graph gives its state back when
@@ -47,11 +56,14 @@ struct RowStats {
 // Digest of `rows` depth rows of n entries.  Depth type T: uint8 (255 =
 // unreached) or int32 (-1 = unreached, mapped to 255).  Optionally writes
 // the uint8 form to out8.
+// With err (device, may be null), its value goes to stats[row].pad.
 template <typename T>
 __global__ void k_row_stats(const T* __restrict__ depth, int64_t n, int rows,
-                            RowStats* __restrict__ stats, uint8_t* __restrict__ out8) {
+                            RowStats* __restrict__ stats, uint8_t* __restrict__ out8,
+                            const int32_t* err) {
   const int row = blockIdx.y;
   if (row >= rows) return;
+  if (err && blockIdx.x == 0 && threadIdx.x == 0) stats[row].pad = (unsigned int)*err;
   const T* d = depth + (int64_t)row * n;
   unsigned long long sum = 0, reached = 0;
   unsigned int mx = 0;
@@ -90,10 +102,13 @@ struct Query {
   uint8_t* out;
   double t_submit, t_start, t_done;
   int batch;
+  bool plain;
 };
 
 struct Inflight {
   bool busy = false;
+  bool plain = false;            // plain single-source searches, not a batch
+  int cls = 0;                   // lane width class of a batch (32 << cls lanes)
   std::vector<Query> q;
   cudaEvent_t done = nullptr;
 };
@@ -105,9 +120,19 @@ struct Slot {
   RowStats* d_stats = nullptr;   // 2 x kMsMaxLanes (one block per batch buffer)
   RowStats* h_stats = nullptr;   // pinned 2 x kMsMaxLanes
   uint8_t* d_plain = nullptr;    // plain mode: uint8 depth row
+  void* h_par = nullptr;         // pinned search parameters: 2 x kMsMaxLanes blocks
   bool admitted = false;
   double last_used = 0;
+  // Device time estimates (ms): one plain search (at admission), and one
+  // batch per lane width class (running); negative while unmeasured.
+  double plain_ms = -1;
+  double batch_ms[4] = {-1, -1, -1, -1};
 };
+
+constexpr size_t kParBlock = 64;   // bytes per parameter block in h_par
+static_assert(kSearchParamBytes <= kParBlock, "parameter block too small");
+constexpr double kEwma = 0.25;     // weight of a new measurement in the estimates
+constexpr int kPlainBusy = 3;      // plain searches only while fewer batches are in flight
 
 }  // namespace
 }  // namespace gbbfs
@@ -159,6 +184,21 @@ bool admit(gbbfs_server* s, size_t idx) {
       if (ms_prepare(sl.g, 1) != GBBFS_OK) return false;
       // Batching keys, once per graph (k = 0: keys only).
       if (s->cfg.order == 0 && ms_order(sl.g, nullptr, 0, nullptr) != GBBFS_OK) return false;
+      // The plain search's cost, once per graph, from the oldest query's
+      // source: the better of two runs (other graphs' work may overlap).
+      if (s->cfg.batches_only == 0 && sl.plain_ms < 0) {
+        for (int rep = 0; rep < 2; rep++) {
+          gbbfs_stats st;
+          memset(&st, 0, sizeof st);
+          if (gbbfs_bfs_device(sl.g, sl.pending.front().source, 15, 18, 1, &st) != GBBFS_OK)
+            return false;
+          if (sl.plain_ms < 0 || st.device_ms < sl.plain_ms) sl.plain_ms = st.device_ms;
+        }
+        // and a 1-source batch's (32 lanes), from its kernel stamps
+        const int32_t src = sl.pending.front().source;
+        if (ms_launch(sl.g, 0, &src, 1) != GBBFS_OK || ms_finish(sl.g, 0) != GBBFS_OK) return false;
+        sl.batch_ms[0] = ms_kernel_ms(sl.g, 0);
+      }
       sl.admitted = true;
       return true;
     }
@@ -194,6 +234,7 @@ void complete(gbbfs_server* s, Slot& sl, Query& q, const RowStats& rs, int statu
   r.checksum = rs.sum;
   r.reached = (int64_t)rs.reached;
   r.max_depth = (int32_t)rs.max_depth;
+  r.plain = q.plain ? 1 : 0;
   std::lock_guard<std::mutex> lk(s->mu);
   s->done.push_back(r);
   s->outstanding--;
@@ -205,17 +246,25 @@ void harvest(gbbfs_server* s, Slot& sl) {
   for (int b = 0; b < 2; b++) {
     Inflight& f = sl.fl[b];
     if (!f.busy || cudaEventQuery(f.done) == cudaErrorNotReady) continue;
-    int st = ms_finish(sl.g, b);
+    int st = f.plain ? GBBFS_OK : ms_finish(sl.g, b);
+    if (!f.plain && st == GBBFS_OK) {
+      const double x = ms_kernel_ms(sl.g, b);
+      double& est = sl.batch_ms[f.cls];
+      if (x > 0) est = est < 0 ? x : (1 - kEwma) * est + kEwma * x;
+    }
     const double t = s->now();
     const size_t n = (size_t)sl.g->n;
     for (size_t i = 0; i < f.q.size(); i++) {
       Query& q = f.q[i];
       q.t_done = t;
-      if (st == GBBFS_OK && q.out)
+      const RowStats& rs = sl.h_stats[kMsMaxLanes * b + i];
+      int qst = st;
+      if (qst == GBBFS_OK && f.plain && rs.pad) qst = (int)rs.pad;
+      if (qst == GBBFS_OK && q.out)
         if (cudaMemcpy(q.out, static_cast<uint8_t*>(ms_depth(sl.g, b)) + i * n, n,
                        cudaMemcpyDeviceToHost) != cudaSuccess)
-          st = GBBFS_ERR_CUDA;
-      complete(s, sl, q, sl.h_stats[kMsMaxLanes * b + i], st);
+          qst = GBBFS_ERR_CUDA;
+      complete(s, sl, q, rs, qst);
     }
     f.q.clear();
     f.busy = false;
@@ -284,21 +333,51 @@ void launch(gbbfs_server* s, Slot& sl) {
       f.q[i].batch = k;
       src[i] = f.q[i].source;
     }
-    int st = ms_launch(sl.g, b, src.data(), k);
-    if (st == GBBFS_OK) {
-      cudaStream_t str = sl.g->stream;
+    int cls = 0;
+    while ((32 << cls) < k) cls++;
+    // Plain searches when k of them are estimated to take less than one
+    // batch of this width (a width not yet measured runs as a batch) and the
+    // GPU is lightly loaded.
+    int in_flight = 0;
+    for (const Slot& o : s->slots)
+      for (const Inflight& x : o.fl) in_flight += (int)(x.busy && !x.plain);
+    const bool plain = s->cfg.batches_only == 0 && in_flight < kPlainBusy && sl.plain_ms > 0 &&
+                       sl.batch_ms[cls] > 0 && (double)k * sl.plain_ms < sl.batch_ms[cls];
+    cudaStream_t str = sl.g->stream;
+    const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
+    int st = GBBFS_OK;
+    if (plain) {
+      // Each search's depths become a uint8 row of buffer b and a digest,
+      // before the next search reuses the handle's arrays.
       cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str);
-      const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
-      k_row_stats<uint8_t><<<dim3(gx, k), 256, 0, str>>>(
-          static_cast<const uint8_t*>(ms_depth(sl.g, b)), sl.g->n, k,
-          sl.d_stats + kMsMaxLanes * b,
-          nullptr);
+      for (int i = 0; i < k && st == GBBFS_OK; i++) {
+        st = bfs_enqueue(sl.g, src[i],
+                         static_cast<char*>(sl.h_par) + ((size_t)b * kMsMaxLanes + i) * kParBlock);
+        if (st != GBBFS_OK) break;
+        k_row_stats<int32_t><<<dim3(gx, 1), 256, 0, str>>>(
+            bfs_depth(sl.g), sl.g->n, 1, sl.d_stats + kMsMaxLanes * b + i,
+            static_cast<uint8_t*>(ms_depth(sl.g, b)) + (size_t)i * sl.g->n,
+            bfs_error_word(sl.g));
+      }
+    } else {
+      st = ms_launch(sl.g, b, src.data(), k);
+      if (st == GBBFS_OK) {
+        cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str);
+        k_row_stats<uint8_t><<<dim3(gx, k), 256, 0, str>>>(
+            static_cast<const uint8_t*>(ms_depth(sl.g, b)), sl.g->n, k,
+            sl.d_stats + kMsMaxLanes * b, nullptr, nullptr);
+      }
+    }
+    for (Query& q : f.q) q.plain = plain;
+    if (st == GBBFS_OK) {
       cudaMemcpyAsync(sl.h_stats + kMsMaxLanes * b, sl.d_stats + kMsMaxLanes * b,
                       sizeof(RowStats) * k,
                       cudaMemcpyDeviceToHost, str);
       ms_mark_copied(sl.g, b, str);
       cudaEventRecord(f.done, str);
       f.busy = true;
+      f.plain = plain;
+      f.cls = cls;
     } else {
       for (Query& q : f.q) {
         q.t_done = s->now();
@@ -317,6 +396,7 @@ void serve_plain(gbbfs_server* s, Slot& sl) {
   sl.pending.pop_front();
   q.t_start = s->now();
   q.batch = 1;
+  q.plain = true;
   int st = gbbfs_bfs_device(sl.g, q.source, 15, 18, 1, nullptr);
   RowStats rs = {0, 0, 0, 0};
   if (st == GBBFS_OK) {
@@ -326,7 +406,7 @@ void serve_plain(gbbfs_server* s, Slot& sl) {
     cudaMemsetAsync(sl.d_stats, 0, sizeof(RowStats), str);
     const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
     k_row_stats<int32_t><<<dim3(gx, 1), 256, 0, str>>>(dp, sl.g->n, 1, sl.d_stats,
-                                                       q.out ? sl.d_plain : nullptr);
+                                                       q.out ? sl.d_plain : nullptr, nullptr);
     cudaMemcpyAsync(sl.h_stats, sl.d_stats, sizeof(RowStats), cudaMemcpyDeviceToHost, str);
     if (q.out) cudaMemcpyAsync(q.out, sl.d_plain, (size_t)sl.g->n, cudaMemcpyDeviceToHost, str);
     if (cudaStreamSynchronize(str) != cudaSuccess) st = GBBFS_ERR_CUDA;
@@ -404,9 +484,11 @@ int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out) {
   s->cfg.max_batch = kMsMaxLanes;
   if (cfg) s->cfg = *cfg;
   if (s->cfg.max_batch <= 0) s->cfg.max_batch = kMsMaxLanes;
-  if ((s->cfg.mode != 0 && s->cfg.mode != 1) || (s->cfg.order != 0 && s->cfg.order != 1)) {
+  if ((s->cfg.mode != 0 && s->cfg.mode != 1) || (s->cfg.order != 0 && s->cfg.order != 1) ||
+      (s->cfg.batches_only != 0 && s->cfg.batches_only != 1)) {
     delete s;
-    last_error() = "server mode must be 0 (batched) or 1 (plain), order 0 (grouped) or 1 (arrival)";
+    last_error() = "server mode must be 0 (batched) or 1 (plain), order 0 (grouped) or 1 "
+                   "(arrival), batches_only 0 or 1";
     return GBBFS_ERR_ARG;
   }
   s->t0 = Clock::now();
@@ -426,6 +508,7 @@ int gbbfs_server_add_graph(gbbfs_server* s, gbbfs_graph* g, int32_t* graph_id) {
   GB_CUDA(cudaMalloc(&sl.d_stats, sizeof(RowStats) * 2 * kMsMaxLanes));
   GB_CUDA(cudaHostAlloc(&sl.h_stats, sizeof(RowStats) * 2 * kMsMaxLanes, cudaHostAllocDefault));
   GB_CUDA(cudaMalloc(&sl.d_plain, std::max<size_t>((size_t)g->n, 256)));
+  GB_CUDA(cudaHostAlloc(&sl.h_par, 2 * kMsMaxLanes * kParBlock, cudaHostAllocDefault));
   for (int b = 0; b < 2; b++)
     GB_CUDA(cudaEventCreateWithFlags(&sl.fl[b].done, cudaEventDisableTiming));
   s->slots.push_back(std::move(sl));
@@ -454,6 +537,7 @@ int gbbfs_server_submit(gbbfs_server* s, int32_t graph_id, int32_t source, uint8
   q.t_submit = s->now();
   q.t_start = q.t_done = 0;
   q.batch = 0;
+  q.plain = false;
   s->inbox.push_back(q);
   s->outstanding++;
   if (ticket) *ticket = q.ticket;
@@ -488,6 +572,7 @@ int gbbfs_server_submit_many(gbbfs_server* s, int64_t count, const int32_t* grap
     q.t_submit = t;
     q.t_start = q.t_done = 0;
     q.batch = 0;
+    q.plain = false;
     s->inbox.push_back(q);
     s->outstanding++;
     if (tickets) tickets[i] = q.ticket;
@@ -534,6 +619,7 @@ int gbbfs_server_close(gbbfs_server* s) {
     cudaFree(sl.d_stats);
     cudaFreeHost(sl.h_stats);
     cudaFree(sl.d_plain);
+    if (sl.h_par) cudaFreeHost(sl.h_par);
     for (int b = 0; b < 2; b++)
       if (sl.fl[b].done) cudaEventDestroy(sl.fl[b].done);
   }

@@ -279,7 +279,10 @@ typedef struct gbbfs_server_config {
                                 holds, batch those with close batching keys
                                 (gbbfs_msbfs_order) around the oldest; 1: strict
                                 arrival order                                   */
-  int32_t pad;
+  int32_t batches_only;      /* mode 0: 0 lets a launch of k queries run as k
+                                plain searches when the graph's measured costs
+                                say they take less than one batch; 1: always a
+                                batch                                           */
 } gbbfs_server_config;
 
 typedef struct gbbfs_result {
@@ -294,7 +297,7 @@ typedef struct gbbfs_result {
   uint64_t checksum;
   int64_t reached;     /* vertices with a depth                                  */
   int32_t max_depth;
-  int32_t pad;
+  int32_t plain;       /* 1 if a plain single-source search answered it          */
 } gbbfs_result;
 
 int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out);

@@ -205,3 +205,41 @@ def test_server_rejects(native, pool):
             srv.add_graph(pool[1][1])
         assert e.value.status == native.ERR_STATE
         srv.drain()
+
+
+@pytest.mark.parametrize("batches_only", [0, 1])
+def test_plain_or_batch_per_launch(native, pool, batches_only):
+    """Launches of few queries may run as plain searches (once the graph's
+    costs are measured), bursts as batches; rows and digests are exact
+    either way, and batches_only keeps every launch a batch."""
+    off, g = pool[1]
+    srcs = [int(s) for s in native.pick_sources(off, 40)]
+    exp = {s: u8(native.DOBFS(g, s, depth=True)[1]) for s in srcs}
+    with native.Server(mode=0, batches_only=batches_only) as srv:
+        srv.add_graph(g)
+        res, rows = [], {}
+        for rnd in range(6):                      # one query at a time
+            s = srcs[rnd]
+            out = np.empty(g.n, np.uint8)
+            rows[srv.submit(0, s, out)] = (s, out)
+            srv.drain()
+            res += srv.poll(16)
+        tickets = srv.submit_many([0] * 300, [srcs[i % 40] for i in range(300)])
+        srv.drain()
+        while True:
+            got = srv.poll(4096)
+            if not got:
+                break
+            res += got
+        assert len(res) == 306
+        for r in res:
+            assert r["status"] == 0
+            assert r["checksum"] == native.depth_checksum(exp[r["source"]])
+        for t, (s, out) in rows.items():
+            assert np.array_equal(out, exp[s])
+        plain = [r for r in res if r["plain"]]
+        if batches_only:
+            assert not plain
+        else:
+            assert plain and all(r["batch_size"] < 256 for r in plain)
+        assert max(r["batch_size"] for r in res) > 32
