@@ -129,7 +129,7 @@ void msbfs_release(MsState* ms) {
 // two frontier buffers, acc; queues q0/q1 with their edge positions qe0/qe1,
 // and tq; two frontier unions and the work-unit table; the search-ordered CSR (offsets counted at 8
 // bytes) and its permutation; the per-vertex depth log (kLogSlots lane masks,
-// levels, flags); depth rows of 128 sources in search order for what the log
+// levels, flags); depth rows of 256 sources in search order for what the log
 // cannot hold and two buffers of rows in original order; slack for the hub
 // list and control blocks.
 size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes) {

@@ -14,7 +14,14 @@
 //                       concatenated adjacency of the queue
 //   tq         int32    vertices whose acc received bits in this level
 //   hubs       int32    vertices of degree > kMsHubDeg, with their chunk prefix
-//   depth      D[k][n]  per-source depth, [source][vertex] order
+//   lvl        u32[n]   depth log: the levels of up to kLogSlots entries per
+//   lmask      L[4n]    vertex (0xff = empty) and the lanes each entry found
+//   spill      u8[n]    1 if some of the vertex's depths are in the rows instead
+//   tflag      u32[n]   touched in this level (128- and 256-lane words)
+//   depth      D[k][s]  rows in search order (stride s) for what the log cannot
+//                       hold: a source's own depth 0, a fifth level, levels
+//                       above 254; k_depth_decode writes the rows callers see
+//                       in original vertex order from the log and these
 //
 // One persistent cooperative kernel runs all levels of a batch.  Level l
 // reads the frontier in fr[l & 1] and writes the next one to fr[(l+1) & 1]:
@@ -33,9 +40,9 @@
 //     tile's unfinished vertices of degree below kMsSmall is streamed 32
 //     edges per lane-step into per-vertex words in shared memory; vertices
 //     up to kMsHubDeg get the whole warp with early exit once every lane is
-//     found.  The warp then writes visit, the depth rows
-//     (coalesced per source), the next frontier words and their fbits word
-//     densely, so no clear or install pass follows.  Hub adjacency is cut
+//     found.  The warp then writes visit, the depth log entries, the next
+//     frontier words and their fbits word densely, so no clear or install
+//     pass follows.  Hub adjacency is cut
 //     into kMsHubChunk-edge items merged into acc and installed after the
 //     barrier.
 // Grid barriers spin on a generation word with a time bound; a barrier that
@@ -537,8 +544,10 @@ __device__ __forceinline__ LaneT warp_gather_or(const int32_t* nbr, const uint32
   return got;
 }
 
-// Resident blocks per SM the register allocation is held to (fewer for the
-// 256-lane word, whose values take twice the registers).
+// Resident blocks per SM the register allocation is held to.  The 256-lane
+// word's values take twice the registers, so it spills a little at 4 blocks
+// (176 bytes of spill stores); it still ran faster there than at 3 or 2,
+// since the kernel is latency-bound and occupancy decides.
 #ifndef GBBFS_MS_MIN_BLOCKS
 #define GBBFS_MS_MIN_BLOCKS 4
 #endif

@@ -1,6 +1,6 @@
 """Batched multi-source BFS from the command line.
 
-    python -m dist_mem_gapbs_gb300.msbfs_cli -g 24 -n 256 --lanes 128 --levels
+    python -m dist_mem_gapbs_gb300.msbfs_cli -g 24 -n 512 --levels
 
 Builds the reference's synthetic graph (-g/-u <scale>, -k <degree>; edge
 list from the host generator, CSR built on the GPU), picks -n sources with
