@@ -43,6 +43,7 @@
 
 #include "engine.h"
 #include "msbfs_kernels.cuh"
+#include "serve_policy.h"
 
 namespace gbbfs {
 
@@ -132,7 +133,6 @@ struct Slot {
 constexpr size_t kParBlock = 64;   // bytes per parameter block in h_par
 static_assert(kSearchParamBytes <= kParBlock, "parameter block too small");
 constexpr double kEwma = 0.25;     // weight of a new measurement in the estimates
-constexpr int kPlainBusy = 3;      // plain searches only while fewer batches are in flight
 
 }  // namespace
 }  // namespace gbbfs
@@ -272,15 +272,9 @@ void harvest(gbbfs_server* s, Slot& sl) {
   }
 }
 
-constexpr size_t kGroupWindow = 4;   // batches' worth of the oldest queries a batch is chosen from
-
 // The queries of a slot's next batch (at most `lanes`): all of them when they
-// fit, or in arrival order when grouping is off.  Otherwise the oldest
-// kGroupWindow * lanes pending queries are sorted (stably) by their sources'
-// batching keys, and the batch is the run of `lanes` consecutive ones in that
-// order with the smallest key spread among the runs that hold the oldest
-// query.  The oldest query always goes, so a query waits for at most as many
-// launches of its graph as there are queries ahead of it.
+// fit, in arrival order when grouping is off, else pick_group's choice from
+// the oldest kGroupWindow * lanes.
 void take_batch(gbbfs_server* s, Slot& sl, size_t lanes, std::vector<Query>& out) {
   const size_t P = sl.pending.size();
   const std::vector<uint16_t>& keys = sl.g->batch_key;
@@ -293,24 +287,10 @@ void take_batch(gbbfs_server* s, Slot& sl, size_t lanes, std::vector<Query>& out
     return;
   }
   const size_t W = std::min(P, kGroupWindow * lanes);
-  auto key = [&](uint32_t i) { return (int)keys[(size_t)sl.pending[i].source]; };
-  std::vector<uint32_t> idx(W);
-  std::iota(idx.begin(), idx.end(), 0u);
-  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return key(a) < key(b); });
-  const size_t p = (size_t)(std::find(idx.begin(), idx.end(), 0u) - idx.begin());
-  const size_t lo = p + 1 >= lanes ? p + 1 - lanes : 0;
-  const size_t hi = std::min(p, W - lanes);
-  size_t best = lo;
-  int best_spread = key(idx[lo + lanes - 1]) - key(idx[lo]);
-  for (size_t st = lo + 1; st <= hi; st++) {
-    const int spread = key(idx[st + lanes - 1]) - key(idx[st]);
-    if (spread < best_spread) {
-      best_spread = spread;
-      best = st;
-    }
-  }
+  std::vector<int> wkeys(W);
+  for (size_t i = 0; i < W; i++) wkeys[i] = (int)keys[(size_t)sl.pending[i].source];
   std::vector<char> take(W, 0);
-  for (size_t j = best; j < best + lanes; j++) take[idx[j]] = 1;
+  for (uint32_t i : pick_group(wkeys, lanes)) take[i] = 1;
   std::vector<Query> rest;
   rest.reserve(W - lanes);
   for (size_t i = 0; i < W; i++) (take[i] ? out : rest).push_back(sl.pending[i]);
@@ -341,8 +321,8 @@ void launch(gbbfs_server* s, Slot& sl) {
     int in_flight = 0;
     for (const Slot& o : s->slots)
       for (const Inflight& x : o.fl) in_flight += (int)(x.busy && !x.plain);
-    const bool plain = s->cfg.batches_only == 0 && in_flight < kPlainBusy && sl.plain_ms > 0 &&
-                       sl.batch_ms[cls] > 0 && (double)k * sl.plain_ms < sl.batch_ms[cls];
+    const bool plain = s->cfg.batches_only == 0 &&
+                       plain_is_cheaper(k, sl.plain_ms, sl.batch_ms[cls], in_flight);
     cudaStream_t str = sl.g->stream;
     const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
     int st = GBBFS_OK;
