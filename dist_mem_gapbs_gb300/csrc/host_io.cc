@@ -28,8 +28,6 @@ int ReadEdgeText(const std::string& path, bool dimacs, int per_edge,
                  std::vector<int32_t>* el) {
   FILE* f = fopen(path.c_str(), "rb");
   if (!f) return GBBFS_ERR_IO;
-  std::vector<char> buf(1 << 20);
-  std::string line;
   char* lp = nullptr;
   size_t cap = 0;
   ssize_t len;

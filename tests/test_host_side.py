@@ -199,3 +199,29 @@ def test_cli_usage_and_missing_input(native):
     assert r.returncode == 0
     assert " -u <scale>  : generate 2^scale uniform-random graph" in r.stdout
     assert "[16]" in r.stdout
+
+
+def test_edge_list_files_malformed(native, tmp_path):
+    """Edge-list parsing: CRLF endings, blank, indented and comment lines are
+    accepted; a record with one number, a negative id, an empty file, an
+    unknown suffix and a missing file are refused."""
+    good = tmp_path / "crlf.el"
+    good.write_bytes(b"# header\r\n\r\n  0 1\r\n\t1 2\r\n% note\r\n2 0\r\n")
+    off, nbr = native.make_graph(filename=str(good), symmetrize=True)
+    ro, rn = _reference_csr(np.array([[0, 1], [1, 2], [2, 0]]))
+    assert np.array_equal(off, ro) and np.array_equal(nbr, rn)
+    for name, body in (("one.el", "0 1\n7\n"), ("neg.el", "0 1\n-2 3\n"),
+                       ("empty.el", ""), ("neg.gr", "a 0 1 5\n")):
+        f = tmp_path / name
+        f.write_text(body)
+        with pytest.raises(native.GbbfsError) as e:
+            native.make_graph(filename=str(f), symmetrize=True)
+        assert e.value.status == native.ERR_IO, name
+    other = tmp_path / "g.txt"
+    other.write_text("0 1\n")
+    with pytest.raises(native.GbbfsError) as e:
+        native.make_graph(filename=str(other), symmetrize=True)
+    assert e.value.status == native.ERR_ARG
+    with pytest.raises(native.GbbfsError) as e:
+        native.make_graph(filename=str(tmp_path / "missing.el"), symmetrize=True)
+    assert e.value.status == native.ERR_IO
