@@ -225,3 +225,23 @@ def test_edge_list_files_malformed(native, tmp_path):
     with pytest.raises(native.GbbfsError) as e:
         native.make_graph(filename=str(tmp_path / "missing.el"), symmetrize=True)
     assert e.value.status == native.ERR_IO
+
+
+def test_abi_argument_checks_without_a_gpu(native):
+    """Calls that fail on their arguments fail before any CUDA call."""
+    L = native.lib()
+    # the batched state's size: a pure function of the graph's shape
+    b1 = native.msbfs_state_bytes(1 << 20, 1 << 24, 1)
+    b4 = native.msbfs_state_bytes(1 << 20, 1 << 24, 4)
+    assert 0 < b1 < b4 < native.msbfs_state_bytes(1 << 21, 1 << 24, 4)
+    assert native.msbfs_state_bytes(1 << 20, 1 << 25, 1) - b1 == 4 * (1 << 24)
+    assert L.gbbfs_msbfs_state_bytes(-1, 0, 1) == -1
+    assert L.gbbfs_msbfs_state_bytes(10, 10, 2) == -1
+    assert L.gbbfs_msbfs_order(None, None, 0, None) == native.ERR_ARG
+    assert L.gbbfs_msbfs_autotune(None, None, 1, 1, None) == native.ERR_ARG
+    assert L.gbbfs_bfs_many(None, None, 1, 15, 18, None, None) == native.ERR_ARG
+    # server configurations outside the documented values
+    for cfg in (dict(mode=2), dict(order=3), dict(batches_only=2)):
+        with pytest.raises(native.GbbfsError) as e:
+            native.Server(**cfg)
+        assert e.value.status == native.ERR_ARG
