@@ -180,7 +180,8 @@ const void* kernel_for(const gbbfs_graph* g, const MsConfig& cfg, int depth_byte
 // slowest source needs, so sources that reach the bulk of the graph at the
 // same level should share a batch.  The proxy for that level is the source's
 // BFS depth from the highest-degree vertex; among sources at the same depth,
-// higher degree reaches the bulk sooner.
+// one whose neighbours have more edges reaches the bulk sooner (the sum of
+// the neighbours' degrees: the number of two-step walks from the source).
 template <typename OffT>
 __global__ void k_argmax_degree(const OffT* off, int64_t n, unsigned long long* best) {
   unsigned long long mine = 0;
@@ -199,14 +200,36 @@ __global__ void k_argmax_degree(const OffT* off, int64_t n, unsigned long long* 
   if ((threadIdx.x & 31) == 0 && mine) atomicMax(best, mine);
 }
 
+// Key of v: hub depth (255 = unreached, else at most 254) << 8, then
+// 255 - q with q = the quarter-octave of s, the sum of v's neighbours'
+// degrees (over the first kKeySample neighbours, scaled by deg / kKeySample,
+// for larger degrees): with t = 4 s and b = its bit length, q = 4 b + the two
+// bits of t below its leading one (0 when s = 0).
+constexpr int kKeySample = 256;
+
 template <typename OffT>
-__global__ void k_batch_keys(const OffT* off, const int32_t* depth, int64_t n, uint16_t* keys) {
+__global__ void k_batch_keys(const OffT* off, const int32_t* nbr, const int32_t* depth,
+                             int64_t n, uint16_t* keys) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     const int32_t d = depth[v];
     const uint32_t hd = d < 0 ? 255u : d > 254 ? 254u : (uint32_t)d;
-    const unsigned long long deg = (unsigned long long)(off[v + 1] - off[v]);
-    keys[v] = (uint16_t)((hd << 8) | (255u - (uint32_t)(deg < 255 ? deg : 255)));
+    const uint64_t b = (uint64_t)off[v], deg = (uint64_t)off[v + 1] - b;
+    const uint64_t take = deg < (uint64_t)kKeySample ? deg : (uint64_t)kKeySample;
+    uint64_t s = 0;
+    for (uint64_t j = 0; j < take; j++) {
+      const int32_t u = nbr[b + j];
+      s += (uint64_t)(off[u + 1] - off[u]);
+    }
+    if (deg > take) s = s * deg / take;
+    uint32_t q = 0;
+    if (s) {
+      const uint64_t t = s << 2;
+      const int bl = 64 - __clzll((long long)t);
+      q = 4u * (uint32_t)bl + (uint32_t)((t >> (bl - 3)) & 3u);
+      if (q > 255u) q = 255u;
+    }
+    keys[v] = (uint16_t)((hd << 8) | (255u - q));
   }
 }
 
@@ -234,7 +257,7 @@ int make_batch_keys(gbbfs_graph* g) {
     const int32_t* depth = nullptr;
     if (rc == GBBFS_OK) rc = gbbfs_result_device_ptrs(g, nullptr, &depth);
     if (rc == GBBFS_OK) {
-      k_batch_keys<OffT><<<4 * g->sms, kThreads, 0, g->stream>>>(off, depth, n, d_keys);
+      k_batch_keys<OffT><<<4 * g->sms, kThreads, 0, g->stream>>>(off, g->nbr, depth, n, d_keys);
       e = cudaGetLastError();
       std::vector<uint16_t> keys((size_t)n);
       if (e == cudaSuccess)

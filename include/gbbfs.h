@@ -235,8 +235,9 @@ int gbbfs_msbfs_device(gbbfs_graph* g, const int32_t* sources, int64_t k, int de
  * of the j-th source to run.  A batch costs about as many full bottom-up
  * levels as its slowest source needs, so sources that reach the bulk of the
  * graph at the same level are put together: sorted (stably) by BFS depth
- * from the highest-degree vertex (lowest id among ties), then by degree,
- * highest first (degrees above 255 tie).  The first call on a handle runs
+ * from the highest-degree vertex (lowest id among ties), then by the sum of
+ * the source's neighbours' degrees, highest first, in quarter-octave steps
+ * (over the first 256 neighbours, scaled, for larger degrees).  The first call on a handle runs
  * that one search (replacing the handle's last single-source result) and
  * keeps two bytes per vertex on the host. */
 int gbbfs_msbfs_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order_out);

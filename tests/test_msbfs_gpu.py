@@ -111,16 +111,13 @@ def test_msbfs_cli(native, capsys):
     assert out.count("batch ") == 2 and "batch 1: 44 sources" in out
 
 
-def test_msbfs_order(native):
+def test_msbfs_order(native, batch_keys):
     """Batching order: stable sort by (depth from the highest-degree vertex,
-    degree highest first, degrees above 255 tied)."""
+    neighbours' degree sum highest first), keys restated in conftest."""
     off, nbr = native.make_graph(15, 16, False)
     with native.Graph(off, nbr) as g:
-        deg = np.diff(off)
-        hub = int(np.argmax(deg))                    # lowest id among the maxima
-        hd = native.DOBFS(g, hub, depth=True)[1]
-        hd = np.where(hd < 0, 255, np.minimum(hd, 254)).astype(np.int64)
-        key = (hd << 8) | (255 - np.minimum(deg, 255))
+        assert np.diff(off).max() > 256             # the sampled-sum path is covered
+        key = batch_keys(native, off, nbr, g)
         srcs = native.pick_sources(off, 500)
         srcs = np.concatenate([srcs, srcs[:7]])      # repeats keep their order
         order = native.msbfs_order(g, srcs)

@@ -123,19 +123,12 @@ def test_full_width_batches(native, pool, max_batch, order):
             assert r["checksum"] == native.depth_checksum(exp[r["source"]])
 
 
-def batch_key(native, off, g):
-    deg = np.diff(off)
-    hd = native.DOBFS(g, int(np.argmax(deg)), depth=True)[1]
-    hd = np.where(hd < 0, 255, np.minimum(hd, 254)).astype(np.int64)
-    return (hd << 8) | (255 - np.minimum(deg, 255))
-
-
-def test_grouped_batches(native, pool):
+def test_grouped_batches(native, pool, batch_keys):
     """With more queries waiting than a batch holds, grouped batches hold
     sources of closer batching keys than arrival-order batches, the oldest
     query goes in the first batch, and every digest is exact."""
     off, g = pool[0]
-    key = batch_key(native, off, g)
+    key = batch_keys(native, off, g.csr()[1], g)
     srcs = [int(s) for s in native.pick_sources(off, 40)]
     exp = {s: u8(native.DOBFS(g, s, depth=True)[1]) for s in srcs}
     rng = np.random.default_rng(5)
