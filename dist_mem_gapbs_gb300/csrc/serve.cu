@@ -326,10 +326,19 @@ void launch(gbbfs_server* s, Slot& sl) {
     cudaStream_t str = sl.g->stream;
     const int gx = std::max(1, std::min(1024, (int)((sl.g->n + 255) / 256)));
     int st = GBBFS_OK;
+    // A failed CUDA call fails the whole launch (its queries end with the
+    // status); work already queued still runs in stream order.
+    auto cuda_ok = [&](cudaError_t e) {
+      if (e != cudaSuccess && st == GBBFS_OK) {
+        last_error() = std::string("query server launch: ") + cudaGetErrorString(e);
+        st = GBBFS_ERR_CUDA;
+      }
+      return st == GBBFS_OK;
+    };
     if (plain) {
       // Each search's depths become a uint8 row of buffer b and a digest,
       // before the next search reuses the handle's arrays.
-      cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str);
+      cuda_ok(cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str));
       for (int i = 0; i < k && st == GBBFS_OK; i++) {
         st = bfs_enqueue(sl.g, src[i],
                          static_cast<char*>(sl.h_par) + ((size_t)b * kMsMaxLanes + i) * kParBlock);
@@ -338,23 +347,26 @@ void launch(gbbfs_server* s, Slot& sl) {
             bfs_depth(sl.g), sl.g->n, 1, sl.d_stats + kMsMaxLanes * b + i,
             static_cast<uint8_t*>(ms_depth(sl.g, b)) + (size_t)i * sl.g->n,
             bfs_error_word(sl.g));
+        cuda_ok(cudaGetLastError());
       }
     } else {
       st = ms_launch(sl.g, b, src.data(), k);
-      if (st == GBBFS_OK) {
-        cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str);
+      if (st == GBBFS_OK &&
+          cuda_ok(cudaMemsetAsync(sl.d_stats + kMsMaxLanes * b, 0, sizeof(RowStats) * k, str))) {
         k_row_stats<uint8_t><<<dim3(gx, k), 256, 0, str>>>(
             static_cast<const uint8_t*>(ms_depth(sl.g, b)), sl.g->n, k,
             sl.d_stats + kMsMaxLanes * b, nullptr, nullptr);
+        cuda_ok(cudaGetLastError());
       }
     }
     for (Query& q : f.q) q.plain = plain;
-    if (st == GBBFS_OK) {
-      cudaMemcpyAsync(sl.h_stats + kMsMaxLanes * b, sl.d_stats + kMsMaxLanes * b,
-                      sizeof(RowStats) * k,
-                      cudaMemcpyDeviceToHost, str);
+    if (st == GBBFS_OK &&
+        cuda_ok(cudaMemcpyAsync(sl.h_stats + kMsMaxLanes * b, sl.d_stats + kMsMaxLanes * b,
+                                sizeof(RowStats) * k, cudaMemcpyDeviceToHost, str))) {
       ms_mark_copied(sl.g, b, str);
-      cudaEventRecord(f.done, str);
+      cuda_ok(cudaEventRecord(f.done, str));
+    }
+    if (st == GBBFS_OK) {
       f.busy = true;
       f.plain = plain;
       f.cls = cls;
