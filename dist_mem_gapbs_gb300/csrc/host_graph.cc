@@ -2,12 +2,14 @@
 // source picking and the bfs_output.txt writer.
 //
 // The graph must be bit-identical to the one the reference's verifier
-// rebuilds, so generation keeps the reference's random streams: std::mt19937
-// reseeded with kRandSeed + block for every 2^18-edge block, libstdc++'s
-// uniform_int_distribution<int32_t> / uniform_real_distribution<float>, and
-// std::shuffle for the R-MAT relabelling (gapbs-verify/generator.h:54-117,
-// src/generator.h:66-167).  Those distributions are implementation-defined,
-// which is why this stays host code linked against libstdc++.
+// rebuilds, so generation keeps the reference's random streams: MT19937
+// reseeded with kRandSeed + block for every 2^18-edge block, the bounded
+// integers and unit floats libstdc++'s uniform_int_distribution<int32_t> /
+// uniform_real_distribution<float> draw from it, and std::shuffle's draws for
+// the R-MAT relabelling (gapbs-verify/generator.h:54-117,
+// src/generator.h:66-167).  Those distributions are implementation-defined;
+// gen_rng.h restates the libstdc++ 13 algorithms, so the graphs do not depend
+// on the library this is built with.
 //
 // The CSR is a function of the edge multiset only (per vertex: sorted,
 // de-duplicated neighbours without self-loops; gapbs-verify/builder.h:137-206),
@@ -20,12 +22,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <random>
 #include <vector>
 
 #include <omp.h>
 
 #include "gbbfs.h"
+#include "gen_rng.h"
 
 namespace {
 
@@ -38,14 +40,14 @@ void GenerateUniform(int64_t nodes, int64_t edges, EdgePair32* el) {
   const int64_t nblocks = (edges + kGenBlock - 1) / kGenBlock;
   #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t b = 0; b < nblocks; b++) {
-    std::mt19937 rng(static_cast<std::mt19937::result_type>(kRandSeed + b));
-    std::uniform_int_distribution<int32_t> pick(0, static_cast<int32_t>(nodes - 1));
+    gbbfs::Mt19937 rng(static_cast<uint32_t>(kRandSeed + b));
+    const uint32_t range = static_cast<uint32_t>(nodes);
     const int64_t lo = b * kGenBlock, hi = std::min(lo + kGenBlock, edges);
     for (int64_t e = lo; e < hi; e++) {
       // The reference's Edge(udist(rng), udist(rng)) is evaluated right to
       // left by g++: the first draw lands in the destination.
-      const int32_t dst = pick(rng);
-      const int32_t src = pick(rng);
+      const int32_t dst = static_cast<int32_t>(gbbfs::bounded(rng, range));
+      const int32_t src = static_cast<int32_t>(gbbfs::bounded(rng, range));
       el[e].u = src;
       el[e].v = dst;
     }
@@ -58,13 +60,12 @@ void GenerateRMat(int scale, int64_t nodes, int64_t edges, EdgePair32* el) {
   const int64_t nblocks = (edges + kGenBlock - 1) / kGenBlock;
   #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t b = 0; b < nblocks; b++) {
-    std::mt19937 rng(static_cast<std::mt19937::result_type>(kRandSeed + b));
-    std::uniform_real_distribution<float> unit(0, 1.0f);
+    gbbfs::Mt19937 rng(static_cast<uint32_t>(kRandSeed + b));
     const int64_t lo = b * kGenBlock, hi = std::min(lo + kGenBlock, edges);
     for (int64_t e = lo; e < hi; e++) {
       int32_t src = 0, dst = 0;
       for (int d = 0; d < scale; d++) {
-        const float p = unit(rng);
+        const float p = gbbfs::unit_float(rng);
         src <<= 1;
         dst <<= 1;
         if (p < ab) {
@@ -82,8 +83,8 @@ void GenerateRMat(int scale, int64_t nodes, int64_t edges, EdgePair32* el) {
   std::vector<int32_t> perm(nodes);
   #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < nodes; i++) perm[i] = static_cast<int32_t>(i);
-  std::mt19937 prng(static_cast<std::mt19937::result_type>(kRandSeed));
-  std::shuffle(perm.data(), perm.data() + nodes, prng);
+  gbbfs::Mt19937 prng(static_cast<uint32_t>(kRandSeed));
+  gbbfs::shuffle_like_libstdcxx(perm.data(), nodes, prng);
   #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < edges; e++) {
     el[e].u = perm[el[e].u];
@@ -241,12 +242,11 @@ int gbbfs_pick_sources(const int64_t* offsets, int64_t n, int64_t given,
     return GBBFS_OK;
   }
   if (offsets[n] == 0) return GBBFS_ERR_ARG;  // every vertex has degree 0
-  std::mt19937 rng(static_cast<std::mt19937::result_type>(kRandSeed));
-  std::uniform_int_distribution<int32_t> pick(0, static_cast<int32_t>(n - 1));
+  gbbfs::Mt19937 rng(static_cast<uint32_t>(kRandSeed));
   for (int i = 0; i < count; i++) {
     int32_t s;
     do {
-      s = pick(rng);
+      s = static_cast<int32_t>(gbbfs::bounded(rng, static_cast<uint32_t>(n)));
     } while (offsets[s + 1] == offsets[s]);
     out[i] = s;
   }
