@@ -48,12 +48,17 @@ struct Mt19937 {
     idx = kN;
   }
 
+  // Word i from words i, i+1 and i+m (indices mod n), in place and in order.
+  GBBFS_HD static uint32_t mix(uint32_t hi, uint32_t lo, uint32_t far) {
+    const uint32_t y = (hi & 0x80000000u) | (lo & 0x7fffffffu);
+    return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+  }
+
   GBBFS_HD void twist() {
-    for (int i = 0; i < kN; i++) {
-      const uint32_t y = (mt[i] & 0x80000000u) | (mt[i + 1 < kN ? i + 1 : 0] & 0x7fffffffu);
-      const int j = i + kM < kN ? i + kM : i + kM - kN;
-      mt[i] = mt[j] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
-    }
+    int i = 0;
+    for (; i < kN - kM; i++) mt[i] = mix(mt[i], mt[i + 1], mt[i + kM]);
+    for (; i < kN - 1; i++) mt[i] = mix(mt[i], mt[i + 1], mt[i + kM - kN]);
+    mt[kN - 1] = mix(mt[kN - 1], mt[0], mt[kM - 1]);
     idx = 0;
   }
 
