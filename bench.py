@@ -164,6 +164,45 @@ def step_alg_bytes(n, step, prev_count):
     return n // 8 + 4 * step["count"]
 
 
+def load_fixture(graph):
+    """The reference's own results for this workload (tests/golden/golden_large.json),
+    or None when the workload has no fixture."""
+    p = os.path.join(ROOT, "tests", "golden", "golden_large.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get(graph)
+
+
+def check_parity(gbbfs, g, sources, fixture):
+    """Outside the timed region: every timed source searched once more through
+    the C ABI, its step trace and the SHA-256 of its depth array compared with
+    the reference's (DOBFS of gapbs-verify, recorded in the fixture)."""
+    import hashlib
+    if fixture is None:
+        return {"fixture": None, "ok": None}
+    by_src = {t["source"]: t for t in fixture["trials"]}
+    depth = np.empty(g.n, np.int32)
+    parent = np.empty(g.n, np.int32)
+    checked = trace_eq = depth_eq = 0
+    missing = 0
+    for s in sources:
+        t = by_src.get(int(s))
+        if t is None:
+            missing += 1
+            continue
+        _, _, st = gbbfs.DOBFS(g, int(s), depth=True, stats=True, parent_out=parent,
+                               depth_out=depth)
+        checked += 1
+        trace_eq += [list(x) for x in st.trace] == t["trace"]
+        depth_eq += hashlib.sha256(depth.tobytes()).hexdigest() == t["depth_sha256"]
+    ok = checked > 0 and trace_eq == checked and depth_eq == checked
+    return {"fixture": "tests/golden/golden_large.json:%s (reference gapbs-verify DOBFS)"
+                       % fixture["flags"], "sources_checked": checked,
+            "trace_equal": trace_eq, "depth_sha256_equal": depth_eq,
+            "sources_without_fixture": missing, "ok": ok}
+
+
 def load_traffic(graph, kernel):
     """DRAM bytes per launch from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -344,6 +383,13 @@ def run_gbbfs(args):
     e2e_secs = [e2e_wall / len(sources)] * len(sources)
     e2e_value = hmean_gteps(e2e_edges, e2e_secs)
 
+    parity = None
+    if rank == 0:
+        fx = load_fixture(args.graph)
+        if fx is not None and (fx["num_nodes"] != n or fx["num_edges_directed"] != m):
+            fx = None
+        parity = check_parity(gbbfs, g, sources, fx)
+
     if tdist is not None:
         t = torch.tensor([my_value, elapsed, e2e_value], dtype=torch.float64, device="cuda")
         allv = [torch.zeros_like(t) for _ in range(world)]
@@ -382,6 +428,7 @@ def run_gbbfs(args):
             "gpu_launches": launches,
             "clocks": clocks.summary(),
             "device_busy_s": busy, "graph_build_s": build_s, "graph_generate_s": gen_s,
+            "parity": parity,
         }
     bc_line = None
     if rank == 0 and world == 1 and not args.no_extras:
@@ -404,6 +451,9 @@ def run_gbbfs(args):
         print(json.dumps(line))
     if tdist is not None:
         tdist.destroy_process_group()
+    if rank == 0 and parity is not None and parity.get("ok") is False:
+        print("bench: depths or step traces differ from the reference's", file=sys.stderr)
+        return 1
     return 0
 
 

@@ -13,8 +13,16 @@ graphs, and records:
   depth array implied by the reference's parent tree;
 * for the two 1024-vertex graphs, the full depth arrays (golden_small.npz).
 
+The large configurations the GPU is measured on (Kronecker-22/24/26 and
+uniform-26, 64 SourcePicker sources each) go to golden_large.json through the
+driver's "fixture" mode: one reference graph build per configuration, the
+hashes computed inside the driver, so no multi-GB array is written out.  The
+same fields are recorded (the depth hash is over the depth the reference's
+parent tree implies).
+
 Run it where the reference checkout exists (not on the GPU host):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # small fixtures
+    python tests/golden/make_golden.py --large    # golden_large.json (~40 min, ~40 GB RAM)
 """
 import hashlib
 import json
@@ -41,6 +49,14 @@ CONFIGS = [
     ("g18", ["-g", "18"]),
 ]
 TRIALS = 8
+
+LARGE_CONFIGS = [
+    ("g22", ["-g", "22"]),
+    ("g24", ["-g", "24"]),
+    ("u26", ["-u", "26"]),
+    ("g26", ["-g", "26"]),
+]
+LARGE_TRIALS = 64
 
 
 def sha(a):
@@ -104,5 +120,56 @@ def main():
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **small)
 
 
+def parse_fixture(stdout):
+    """graph line, source list and per-trial records of the driver's fixture mode."""
+    graph, sources, trials, trace = None, None, [], None
+    for line in stdout.splitlines():
+        f = line.split()
+        if not f:
+            continue
+        if f[0] == "graph":
+            graph = dict(num_nodes=int(f[1]), num_edges_directed=int(f[2]),
+                         offsets_sha256=f[3], neigh_sha256=f[4])
+        elif f[0] == "sources":
+            sources = [int(x) for x in f[1:]]
+        elif f[0] == "Source:":
+            trace = []
+        elif f[0] in ("td", "bu") and trace is not None:
+            trace.append([f[0], int(f[1])])
+        elif f[0] in ("e", "c") and trace is not None:
+            trace.append([f[0], 0])
+        elif f[0] == "result":
+            trials.append(dict(source=int(f[1]), reached=int(f[2]),
+                               reached_degree_sum=int(f[3]), max_depth=int(f[4]),
+                               depth_sha256=f[5], trace=trace))
+            trace = None
+    return graph, sources, trials
+
+
+def main_large(names=None):
+    obuild.build_ref()
+    if not O.ref_available():
+        raise SystemExit("reference sources not present: cannot regenerate fixtures")
+    path = os.path.join(HERE, "golden_large.json")
+    out = {}
+    if os.path.exists(path):
+        with open(path) as f:
+            out = json.load(f)
+    for name, flags in LARGE_CONFIGS:
+        if names and name not in names:
+            continue
+        with tempfile.TemporaryDirectory() as d:
+            stdout = O.ref_run("fixture", d + "/f", flags + ["-n", str(LARGE_TRIALS)])
+        graph, sources, trials = parse_fixture(stdout)
+        assert len(trials) == LARGE_TRIALS and sources == [t["source"] for t in trials]
+        out[name] = dict(flags=flags, sources=sources, trials=trials, **graph)
+        print(name, graph["num_nodes"], graph["num_edges_directed"], flush=True)
+        with open(path, "w") as f:
+            json.dump(out, f, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
-    main()
+    if "--large" in sys.argv:
+        main_large([a for a in sys.argv[1:] if not a.startswith("--")])
+    else:
+        main()
