@@ -22,10 +22,13 @@ enum : int32_t {
   kKindBU = GBBFS_STEP_BU,
   kKindC = GBBFS_STEP_C,
   kKindStop = 5,
+  kKindTDB = 6,   // a top-down step run as claims into a bitmap, then a sweep (k_tdb)
 };
 
 // Branches of the per-step switch node.
-enum : unsigned { kSelTD = 0, kSelQ2B = 1, kSelBU0 = 2, kSelBU1 = 3, kSelB2Q = 4, kSelNone = 5 };
+enum : unsigned {
+  kSelTD = 0, kSelQ2B = 1, kSelBU0 = 2, kSelBU1 = 3, kSelB2Q = 4, kSelTDB = 5, kSelNone = 6
+};
 
 // Device-side counters of the current step.  qpacked[i] describes frontier
 // queue i: (vertex count << shift) | (sum of their out-degrees).  One 64-bit

@@ -141,7 +141,8 @@ int setup_grids(gbbfs_graph* g) {
   GB_TRY(occupancy_grid((const void*)k_td<OffT>, g->sms, &g->grid_td));
   GB_TRY(occupancy_grid((const void*)k_bu<OffT, 0>, g->sms, &g->grid_bu));
   GB_TRY(occupancy_grid((const void*)k_q2b<OffT>, g->sms, &g->grid_q2b));
-  GB_TRY(occupancy_grid((const void*)k_b2q<OffT>, g->sms, &g->grid_b2q));
+  GB_TRY(occupancy_grid((const void*)k_b2q<OffT, false>, g->sms, &g->grid_b2q));
+  GB_TRY(occupancy_grid((const void*)k_tdb<OffT>, g->sms, &g->grid_tdb));
   return GBBFS_OK;
 }
 
@@ -282,7 +283,7 @@ int build_graph(gbbfs_graph* g) {
   cudaGraphNodeParams sp = {cudaGraphNodeTypeConditional};
   sp.conditional.handle = h_sel;
   sp.conditional.type = cudaGraphCondTypeSwitch;
-  sp.conditional.size = 5;
+  sp.conditional.size = 6;
   cudaGraphNode_t switch_node;
   GB_CUDA(cudaGraphAddNode(&switch_node, body, &decide_node, nullptr, 1, &sp));
   cudaGraphNode_t k;
@@ -295,7 +296,12 @@ int build_graph(gbbfs_graph* g) {
   GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelBU1], nullptr, 0,
                     (const void*)k_bu<OffT, 1>, g->grid_bu, kThreads, args_b));
   GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelB2Q], nullptr, 0,
-                    (const void*)k_b2q<OffT>, g->grid_b2q, kThreads, args_b));
+                    (const void*)k_b2q<OffT, false>, g->grid_b2q, kThreads, args_b));
+  cudaGraphNode_t tdb;
+  GB_TRY(add_kernel(&tdb, sp.conditional.phGraph_out[kSelTDB], nullptr, 0,
+                    (const void*)k_tdb<OffT>, g->grid_tdb, kThreads, args_b));
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelTDB], &tdb, 1,
+                    (const void*)k_b2q<OffT, true>, g->grid_b2q, kThreads, args_b));
 
   cudaGraphNode_t copy_node;
   GB_CUDA(cudaGraphAddMemcpyNode1D(&copy_node, graph, &loop_node, 1, g->h_st, g->st,
@@ -400,6 +406,10 @@ int run_stepped(gbbfs_graph* g, std::vector<double>* kernel_seconds) {
     GB_TRY(step_event(g, 2 * steps));
     switch (kind) {
       case kKindTD: k_td<OffT><<<g->grid_td, kThreads, 0, s>>>(b); break;
+      case kKindTDB:
+        k_tdb<OffT><<<g->grid_tdb, kThreads, 0, s>>>(b);
+        k_b2q<OffT, true><<<g->grid_b2q, kThreads, 0, s>>>(b);
+        break;
       case kKindE: k_q2b<OffT><<<g->grid_q2b, kThreads, 0, s>>>(b); break;
       case kKindBU:
         if (g->h_st->parity)
@@ -407,7 +417,7 @@ int run_stepped(gbbfs_graph* g, std::vector<double>* kernel_seconds) {
         else
           k_bu<OffT, 0><<<g->grid_bu, kThreads, 0, s>>>(b);
         break;
-      case kKindC: k_b2q<OffT><<<g->grid_b2q, kThreads, 0, s>>>(b); break;
+      case kKindC: k_b2q<OffT, false><<<g->grid_b2q, kThreads, 0, s>>>(b); break;
       default:
         g_last_error = "unknown step kind from the device";
         return GBBFS_ERR_STATE;

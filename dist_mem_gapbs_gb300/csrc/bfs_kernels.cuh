@@ -33,36 +33,44 @@ namespace gbbfs {
 // The reference keeps -out_degree in parent for unvisited vertices so that
 // scout_count can sum it; here the degree is read from the offsets at claim
 // time instead, which keeps the init a pure store stream.
+//
+// The -1 fill is a TMA bulk store: each CTA fills a 16 KB tile of -1 in
+// shared memory once, and one thread issues cp.async.bulk stores of that tile
+// over the CTA's share of parent (and depth), 16 KB per instruction, then
+// waits for them to complete.  The other threads meanwhile write the bitmaps.
+// The source's own entries are written by k_decide's first call, after this
+// kernel has completed, so no generic store races the bulk stores.
+// (Every parent/depth array is 32 W entries from cudaMalloc or a 256-aligned
+// slice: the addresses are 16-byte aligned and 128 W bytes is a multiple of 16.)
+constexpr int kFillTile = 16384;
 template <typename OffT>
 __global__ void __launch_bounds__(kThreads) k_init(Bufs<OffT> b) {
+  __shared__ __align__(128) int4 neg_tile[kFillTile / 16];
   DevState* st = b.st;
   stamp_begin(st);
   const int32_t source = st->source;
-  int32_t* parent = st->parent;
-  int32_t* depth = st->want_depth ? b.depth : nullptr;
+  unsigned char* parent = reinterpret_cast<unsigned char*>(st->parent);
+  unsigned char* depth = st->want_depth ? reinterpret_cast<unsigned char*>(b.depth) : nullptr;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // parent / depth: 8 int32 per thread-iteration (two 16-byte stores).
-  const int64_t nvec = b.W * 4;
-  const int64_t src_vec = source >> 3;
-  const int src_lane = source & 7;
-  auto put = [](int4 v, int lane, int val) {
-    v.x = lane == 0 ? val : v.x;
-    v.y = lane == 1 ? val : v.y;
-    v.z = lane == 2 ? val : v.z;
-    v.w = lane == 3 ? val : v.w;
-    return v;
-  };
-  const int4 neg = make_int4(-1, -1, -1, -1);
-  for (int64_t i = tid; i < nvec; i += stride) {
-    const bool here = i == src_vec;
-    const int la = here ? src_lane : -1, lb = here ? src_lane - 4 : -1;
-    reinterpret_cast<int4*>(parent)[2 * i] = put(neg, la, source);
-    reinterpret_cast<int4*>(parent)[2 * i + 1] = put(neg, lb, source);
-    if (depth) {
-      reinterpret_cast<int4*>(depth)[2 * i] = put(neg, la, 0);
-      reinterpret_cast<int4*>(depth)[2 * i + 1] = put(neg, lb, 0);
+  for (int i = threadIdx.x; i < kFillTile / 16; i += blockDim.x)
+    neg_tile[i] = make_int4(-1, -1, -1, -1);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t tile = (uint32_t)__cvta_generic_to_shared(neg_tile);
+    const uint64_t total = (uint64_t)b.W * 128;   // bytes of 32 W int32 entries
+    for (uint64_t o = (uint64_t)blockIdx.x * kFillTile; o < total;
+         o += (uint64_t)gridDim.x * kFillTile) {
+      const uint32_t sz = (uint32_t)(total - o < (uint64_t)kFillTile ? total - o : kFillTile);
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                   :: "l"(parent + o), "r"(tile), "r"(sz) : "memory");
+      if (depth)
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                     :: "l"(depth + o), "r"(tile), "r"(sz) : "memory");
     }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
   const int64_t src_word = source >> 5;
   for (int64_t w = tid; w < b.W; w += stride) {
@@ -106,6 +114,13 @@ __global__ void __launch_bounds__(kThreads) k_init(Bufs<OffT> b) {
 // top-down or bottom-up step continues the loop only after claiming a vertex,
 // and at most two conversions sit between two such steps) stops a run-away
 // loop with GBBFS_ERR_TIMEOUT instead of spinning.
+// Top-down steps whose frontier has more than n >> kTdBitmapShift edges run
+// as k_tdb + sweep instead of k_td.
+#ifndef GBBFS_TDB_SHIFT
+#define GBBFS_TDB_SHIFT 3
+#endif
+constexpr int kTdBitmapShift = GBBFS_TDB_SHIFT;
+
 template <typename OffT>
 __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
                          cudaGraphConditionalHandle h_sel) {
@@ -131,6 +146,9 @@ __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
   switch (s->next_kind) {
     case kKindInit: {
       s->init_ns = ns;
+      // The source's own entries, after k_init's bulk -1 stores completed.
+      s->parent[s->source] = s->source;
+      if (s->want_depth) b.depth[s->source] = 0;
       const unsigned long long p = c->qpacked[0];
       s->F = (int64_t)(p >> b.shift);
       s->scout = (int64_t)(p & emask);
@@ -138,7 +156,8 @@ __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
       frontier_decision = true;
       break;
     }
-    case kKindTD: {
+    case kKindTD:
+    case kKindTDB: {
       const int nxt = s->cur ^ 1;
       const unsigned long long p = c->qpacked[nxt];
       s->F = (int64_t)(p >> b.shift);
@@ -185,7 +204,9 @@ __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
       next = kKindE;
     } else {
       s->edges_to_check -= s->scout;
-      next = kKindTD;
+      // A frontier with many edges claims many vertices: its step runs as
+      // claims into a bitmap and a sweep that builds the next queue (k_tdb).
+      next = s->scout > (b.n >> kTdBitmapShift) ? kKindTDB : kKindTD;
     }
   }
   if (++s->iter > s->max_iter && next != kKindStop) {
@@ -196,7 +217,7 @@ __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
     s->old_awake = s->awake;
     c->awake = 0;
     c->scanned = 0;
-  } else if (next == kKindTD) {
+  } else if (next == kKindTD || next == kKindTDB) {
     c->qpacked[s->cur ^ 1] = 0;
   } else if (next == kKindC) {
     c->qpacked[s->cur] = 0;
@@ -207,6 +228,7 @@ __global__ void k_decide(Bufs<OffT> b, cudaGraphConditionalHandle h_loop,
   if (s->in_graph) {
     unsigned sel = kSelNone;
     if (next == kKindTD) sel = kSelTD;
+    else if (next == kKindTDB) sel = kSelTDB;
     else if (next == kKindE) sel = kSelQ2B;
     else if (next == kKindBU) sel = s->parity ? kSelBU1 : kSelBU0;
     else if (next == kKindC) sel = kSelB2Q;
@@ -415,6 +437,112 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
 }
 
 // ---------------------------------------------------------------------------
+// Top-down step for frontiers with many edges (TDStep, gapbs-verify/bfs.cc:67-89,
+// src/bfs.cc:81-100, as k_td splits it over warps).  Where a step claims
+// millions of vertices, k_td's claim path is the cost: each claim waits on an
+// atomicOr's returned value, then stages the vertex and later loads its
+// degree.  Here a neighbour v not yet in visited (as of the step's start) or
+// in the claim bitmap bm[parity] gets its bit set there by an atomicOr whose
+// result is not used (a reduction: no round trip), and parent[v] = u.  Two
+// frontier vertices may both reach v in the same step; each then stores
+// itself as v's parent, and the last store stands: both are v's neighbours
+// one level up, as the reference's own racing compare-and-swap allows.  The
+// sweep that follows (k_b2q<OffT, true>) turns the bitmap into the next queue
+// in vertex order, with degree prefix, packed counter and visited update, so
+// the step's count and scout_count are the reference's exactly.
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_tdb(Bufs<OffT> b) {
+  DevState* st = b.st;
+  stamp_begin(st);
+  const int cur = st->cur;
+  const int level = st->level;
+  int32_t* parent = st->parent;
+  int32_t* depth = st->want_depth ? b.depth : nullptr;
+  const int32_t* qv = cur ? b.qv1 : b.qv0;
+  const OffT* qs = cur ? b.qs1 : b.qs0;
+  const OffT* __restrict__ off = b.off;
+  const int32_t* __restrict__ nbr = b.nbr;
+  const uint32_t* visited = b.visited;
+  uint32_t* claim = st->parity ? b.bm1 : b.bm0;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long packed = b.ctr->qpacked[cur];
+  const int64_t F = (int64_t)(packed >> b.shift);
+  const uint64_t E = packed & ((1ull << b.shift) - 1);
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t nchunks = (E + 31) >> 5;
+  const uint64_t per = (nchunks + nwarps - 1) / nwarps;
+  const uint64_t c_begin = warp * per;
+  const uint64_t c_end = c_begin + per < nchunks ? c_begin + per : nchunks;
+  auto visit = [&](int32_t v, int32_t u) {
+    const uint32_t bit = 1u << (v & 31);
+    const uint32_t seen = __ldcg(visited + (v >> 5)) | __ldcg(claim + (v >> 5));
+    if (!(seen & bit)) {
+      atomicOr(claim + (v >> 5), bit);
+      parent[v] = u;
+      if (depth) depth[v] = level;
+    }
+  };
+  if (c_begin < c_end) {
+    uint64_t e0 = c_begin << 5;
+    int64_t lo = 0, hi = F - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if ((uint64_t)qs[mid] <= e0) lo = mid; else hi = mid - 1;
+    }
+    int64_t i0 = lo;
+    int64_t ij = -1;
+    uint64_t sj = ~0ull;
+    int32_t uj = 0;
+    uint64_t rj = 0;
+    for (uint64_t c = c_begin; c < c_end; c++, e0 += 32) {
+      if (ij != i0 + lane) {
+        ij = i0 + lane;
+        sj = ~0ull;
+        uj = 0;
+        rj = 0;
+        if (ij < F) {
+          sj = (uint64_t)qs[ij];
+          uj = qv[ij];
+          rj = (uint64_t)off[uj];
+        }
+      }
+      const uint64_t s_next = shfl(sj, 1);
+      if (c + kHub <= c_end && s_next >= e0 + 32 * kHub) {
+        const int32_t u = __shfl_sync(kFull, uj, 0);
+        const uint64_t base_nb = shfl(rj, 0) + (e0 - shfl(sj, 0)) + lane;
+        int32_t v[kHub];
+#pragma unroll
+        for (int q = 0; q < kHub; q++)
+          v[q] = e0 + 32 * q + lane < E ? __ldg(nbr + base_nb + 32 * q) : -1;
+#pragma unroll
+        for (int q = 0; q < kHub; q++)
+          if (v[q] >= 0) visit(v[q], u);
+        if (s_next == e0 + 32 * kHub) i0 += 1;
+        c += kHub - 1;
+        e0 += 32 * (kHub - 1);
+        continue;
+      }
+      unsigned mybit = 0;
+      if (lane == 0) mybit = 1u;
+      else if (ij < F && sj < e0 + 32) mybit = 1u << (unsigned)(sj - e0);
+      const unsigned starts = __reduce_or_sync(kFull, mybit);
+      const int k = __popc(starts & (kFull >> (31 - lane))) - 1;
+      const int32_t u = __shfl_sync(kFull, uj, k);
+      const uint64_t s = shfl(sj, k);
+      const uint64_t r = shfl(rj, k);
+      const uint64_t e = e0 + lane;
+      if (e < E) visit(__ldg(nbr + (r + (e - s))), u);
+      const unsigned le = __ballot_sync(kFull, lane == 0 || (ij < F && sj <= e0 + 32));
+      int adv = __popc(le) - 1;
+      if (le == kFull && i0 + 32 < F && (uint64_t)qs[i0 + 32] == e0 + 32) adv = 32;
+      i0 += adv;
+    }
+  }
+  stamp_end(st);
+}
+
+// ---------------------------------------------------------------------------
 // QueueToBitmap (gapbs-verify/bfs.cc:92-98, src/bfs.cc:104-112): set the bit
 // of every queue entry in the bottom-up frontier bm[parity] (all zero on
 // entry: BitmapToQueue clears what it reads, and the init clears bm0).
@@ -595,13 +723,16 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
 // bit of the frontier bm[parity] becomes an entry of queue `cur` (with its
 // degree prefix), and the bitmap is cleared on the way so it is all-zero for
 // the next QueueToBitmap.  Thread per word; one atomic per CTA-iteration.
-template <typename OffT>
+//
+// kAfterTd: the sweep after k_tdb.  The bitmap holds that step's claims; they
+// go to the next queue (cur ^ 1) and into visited.
+template <typename OffT, bool kAfterTd>
 __global__ void __launch_bounds__(kThreads) k_b2q(Bufs<OffT> b) {
   __shared__ unsigned long long warp_tot[kWarpsPerCta];
   __shared__ unsigned long long cta_base;
   DevState* st = b.st;
-  stamp_begin(st);
-  const int dst = st->cur;
+  if (!kAfterTd) stamp_begin(st);
+  const int dst = kAfterTd ? st->cur ^ 1 : st->cur;
   uint32_t* front = st->parity ? b.bm1 : b.bm0;
   int32_t* qv_out = dst ? b.qv1 : b.qv0;
   OffT* qs_out = dst ? b.qs1 : b.qs0;
@@ -617,7 +748,10 @@ __global__ void __launch_bounds__(kThreads) k_b2q(Bufs<OffT> b) {
     uint32_t bits = 0;
     if (w < W) {
       bits = front[w];
-      if (bits) front[w] = 0;
+      if (bits) {
+        front[w] = 0;
+        if (kAfterTd) b.visited[w] |= bits;
+      }
     }
     unsigned long long degsum = 0;
     for (uint32_t x = bits; x; x &= x - 1) {

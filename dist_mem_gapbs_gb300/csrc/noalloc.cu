@@ -155,12 +155,13 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   b.W = (n + 31) / 32;
   b.shift = shift;
 
-  int g_init = 0, g_td = 0, g_bu = 0, g_q2b = 0, g_b2q = 0;
+  int g_init = 0, g_td = 0, g_bu = 0, g_q2b = 0, g_b2q = 0, g_tdb = 0;
   GB_TRY(occupancy((const void*)k_init<OffT>, sms, &g_init));
   GB_TRY(occupancy((const void*)k_td<OffT>, sms, &g_td));
   GB_TRY(occupancy((const void*)k_bu<OffT, 0>, sms, &g_bu));
   GB_TRY(occupancy((const void*)k_q2b<OffT>, sms, &g_q2b));
-  GB_TRY(occupancy((const void*)k_b2q<OffT>, sms, &g_b2q));
+  GB_TRY(occupancy((const void*)k_b2q<OffT, false>, sms, &g_b2q));
+  GB_TRY(occupancy((const void*)k_tdb<OffT>, sms, &g_tdb));
 
   // Start from a clean control block (the previous call left its own state),
   // with the timer stamps at their neutral values.
@@ -195,6 +196,10 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
     if (kind == kKindStop) break;
     switch (kind) {
       case kKindTD: k_td<OffT><<<g_td, kThreads, 0, s>>>(b); break;
+      case kKindTDB:
+        k_tdb<OffT><<<g_tdb, kThreads, 0, s>>>(b);
+        k_b2q<OffT, true><<<g_b2q, kThreads, 0, s>>>(b);
+        break;
       case kKindE: k_q2b<OffT><<<g_q2b, kThreads, 0, s>>>(b); break;
       case kKindBU:
         if (parity)
@@ -202,7 +207,7 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
         else
           k_bu<OffT, 0><<<g_bu, kThreads, 0, s>>>(b);
         break;
-      case kKindC: k_b2q<OffT><<<g_b2q, kThreads, 0, s>>>(b); break;
+      case kKindC: k_b2q<OffT, false><<<g_b2q, kThreads, 0, s>>>(b); break;
       default:
         last_error() = "unknown step kind from the device";
         return GBBFS_ERR_STATE;
