@@ -2,8 +2,9 @@
 //
 // Formats follow the reference's Reader / Writer: ".sg" serialized graphs
 // (src/writer.h:39-69, src/reader.h:291-345), ".el" and ".wel" edge lists,
-// DIMACS ".gr" files (gapbs-verify/reader.h:49-84) and Matrix Market ".mtx"
-// coordinate files (src/reader.h:186-256).  Edge lists go through
+// DIMACS ".gr" files (gapbs-verify/reader.h:49-84), METIS ".graph" files
+// (gapbs-verify/reader.h:88-140) and Matrix Market ".mtx" coordinate files
+// (src/reader.h:186-256).  Edge lists go through
 // gbbfs_build_csr, the same construction the synthetic graphs use.
 
 #include <cstdint>
@@ -142,6 +143,75 @@ int ReadMTX(const std::string& path, std::vector<int32_t>* el, bool* undirected)
   return rc;
 }
 
+// METIS graph files (gapbs-verify/reader.h:88-140, src/reader.h ".graph"): '%'
+// comment lines; a header "num_nodes num_edges [fmt]" with fmt 1 for edge
+// weights (0 or 100: none; other codes are refused); then one line per vertex
+// u (1-based neighbour ids, "neighbour weight" pairs when weighted), an empty
+// line being a vertex without neighbours.  Every entry of a line is read.
+// (The reference's own loop drops a line's last entry unless whitespace
+// follows it; files whose lines end in a space read the same in both.)
+int ReadMetis(const std::string& path, std::vector<int32_t>* el) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return GBBFS_ERR_IO;
+  char* lp = nullptr;
+  size_t cap = 0;
+  int rc = GBBFS_OK;
+  bool header = false, weighted = false;
+  long long num_nodes = 0, u = 0;
+  while (rc == GBBFS_OK && (!header || u < num_nodes) && getline(&lp, &cap, f) >= 0) {
+    if (lp[0] == '%') continue;
+    const char* p = lp;
+    char* end = nullptr;
+    if (!header) {
+      num_nodes = strtoll(p, &end, 10);
+      if (end == p || num_nodes < 0 || num_nodes > INT32_MAX) {
+        rc = GBBFS_ERR_IO;
+        break;
+      }
+      p = end;
+      (void)strtoll(p, &end, 10);   // num_edges: not needed
+      if (end == p) {
+        rc = GBBFS_ERR_IO;
+        break;
+      }
+      p = end;
+      const long long fmt = strtoll(p, &end, 10);
+      if (end != p) {
+        if (fmt == 1)
+          weighted = true;
+        else if (fmt != 0 && fmt != 100)
+          rc = GBBFS_ERR_IO;
+      }
+      header = true;
+      continue;
+    }
+    for (;;) {
+      const long long v = strtoll(p, &end, 10);
+      if (end == p) break;
+      p = end;
+      if (weighted) {
+        (void)strtoll(p, &end, 10);
+        if (end == p) {
+          rc = GBBFS_ERR_IO;
+          break;
+        }
+        p = end;
+      }
+      if (v < 1 || v - 1 > INT32_MAX) {
+        rc = GBBFS_ERR_IO;
+        break;
+      }
+      el->push_back(static_cast<int32_t>(u));
+      el->push_back(static_cast<int32_t>(v - 1));
+    }
+    u++;
+  }
+  if (rc == GBBFS_OK && !header) rc = GBBFS_ERR_IO;
+  free(lp);
+  fclose(f);
+  return rc;
+}
+
 int ReadSG(const std::string& path, int64_t** offsets_out, int32_t** neigh_out,
            int64_t* n_out, int64_t* m_out) {
   FILE* f = fopen(path.c_str(), "rb");
@@ -204,7 +274,10 @@ int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
     rc = ReadEdgeText(p, true, 3, &el);
   else if (suf == ".mtx")
     rc = ReadMTX(p, &el, &undirected);
-  else
+  else if (suf == ".graph") {
+    rc = ReadMetis(p, &el);
+    undirected = true;   // METIS lists every edge on both endpoints' lines
+  } else
     return GBBFS_ERR_ARG;
   if (rc != GBBFS_OK) return rc;
   // directed graphs are outside this engine; a symmetric .mtx is undirected

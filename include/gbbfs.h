@@ -355,10 +355,12 @@ int gbbfs_build_csr(int32_t* el_pairs, int64_t edges, int64_t num_nodes,
 /* Read a graph file the way Builder::MakeGraph does for -f
  * (src/reader.h:57-257, :291-345): ".sg" serialized graphs (undirected only),
  * ".el" / ".wel" edge lists ("u v [w]" per line, weights ignored) and DIMACS
- * ".gr" ("a u v w" lines, 1-based ids) and Matrix Market ".mtx" coordinate
- * files (src/reader.h:186-256; 1-based, values ignored).  Edge lists must be
- * symmetrized (symmetrize != 0, the -s flag) unless the file says it is
- * symmetric: this engine runs on undirected CSR only. */
+ * ".gr" ("a u v w" lines, 1-based ids), METIS ".graph" files (one line of
+ * 1-based neighbours per vertex, gapbs-verify/reader.h:88-140; undirected by
+ * the format) and Matrix Market ".mtx" coordinate files (src/reader.h:186-256;
+ * 1-based, values ignored).  Edge lists must be symmetrized (symmetrize != 0,
+ * the -s flag) unless the file says it is symmetric: this engine runs on
+ * undirected CSR only. */
 int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
                      int32_t** neigh_out, int64_t* n_out, int64_t* m_dir_out);
 

@@ -20,13 +20,27 @@ hashes computed inside the driver, so no multi-GB array is written out.  The
 same fields are recorded (the depth hash is over the depth the reference's
 parent tree implies).
 
-Run it where the reference checkout exists (not on the GPU host):
+Two more fixture files pin the rows around the search:
+
+* golden_bc.json: BC's BFS phase, the reference's PBFS (gapbs-verify/bc.cc:51-92,
+  driven by oracle/ref_bc_driver.cc): per source the SHA-256 of the depths, of
+  the path counts (as uint64, exact below 2^53) and of the successor bits,
+  and the level sizes;
+* golden_io.json: the graph files under tests/golden/io/ (edge lists, DIMACS,
+  Matrix Market, METIS and a serialized graph, all made here from seeded
+  random graphs), each read by the reference's Reader through Builder (-f,
+  with -s where the format needs it), with the SHA-256 of the CSR it builds.
+
+Run it where a copy of the reference sources is present (not on the GPU host):
     python tests/golden/make_golden.py            # small fixtures
     python tests/golden/make_golden.py --large    # golden_large.json (~40 min, ~40 GB RAM)
+    python tests/golden/make_golden.py --bc       # golden_bc.json
+    python tests/golden/make_golden.py --io       # tests/golden/io/ and golden_io.json
 """
 import hashlib
 import json
 import os
+import subprocess
 import sys
 import tempfile
 
@@ -168,8 +182,128 @@ def main_large(names=None):
             json.dump(out, f, indent=1, sort_keys=True)
 
 
+BC_CONFIGS = [
+    ("g10", ["-g", "10"]),
+    ("u12", ["-u", "12"]),
+    ("g14k8", ["-g", "14", "-k", "8"]),
+    ("g16", ["-g", "16"]),
+]
+BC_TRIALS = 8
+
+
+def main_bc():
+    obuild.build_ref()
+    exe = os.path.join(obuild.REF_OUT, "gapbs_ref_bc")
+    if not os.path.exists(exe):
+        raise SystemExit("reference sources not present: cannot regenerate fixtures")
+    out = {}
+    for name, flags in BC_CONFIGS:
+        r = subprocess.run([exe] + flags + ["-n", str(BC_TRIALS)], capture_output=True,
+                           text=True, check=True)
+        trials = []
+        for line in r.stdout.splitlines():
+            f = line.split()
+            if f and f[0] == "bcbfs":
+                trials.append(dict(source=int(f[1]), reached=int(f[2]), levels=int(f[3]),
+                                   counts_exact=bool(int(f[4])), depth_sha256=f[5],
+                                   path_counts_sha256=f[6], succ_bits_sha256=f[7],
+                                   level_sizes=[int(x) for x in f[8].split(",")]))
+        assert len(trials) == BC_TRIALS
+        out[name] = dict(flags=flags, trials=trials)
+        print(name, [t["source"] for t in trials])
+    with open(os.path.join(HERE, "golden_bc.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
+IO_DIR = os.path.join(HERE, "io")
+
+
+def write_io_inputs():
+    """Small graph files in every format the reference's Reader takes, from a
+    seeded random multigraph (duplicates, self-loops, an isolated vertex)."""
+    rng = np.random.default_rng(20240611)
+    n = 300
+    el = rng.integers(0, n, size=(1500, 2))
+    el = el[(el[:, 0] != 150) & (el[:, 1] != 150)]                 # 150 is isolated
+    el = np.concatenate([el, el[:40], [[7, 7], [8, 8]], [[n - 1, 3]]])
+    w = rng.integers(1, 100, size=len(el))
+    os.makedirs(IO_DIR, exist_ok=True)
+    files = {}
+
+    def put(name, text):
+        with open(os.path.join(IO_DIR, name), "w") as fh:
+            fh.write(text)
+        files[name] = None
+
+    put("er.el", "".join("%d %d\n" % (u, v) for u, v in el))
+    put("er.wel", "".join("%d %d %d\n" % (u, v, x) for (u, v), x in zip(el, w)))
+    put("er.gr", "c seeded random multigraph\np sp %d %d\n" % (n, len(el)) +
+        "".join("a %d %d %d\n" % (u + 1, v + 1, x) for (u, v), x in zip(el, w)))
+    put("er_general.mtx", "%%%%MatrixMarket matrix coordinate pattern general\n"
+        "%% seeded random multigraph\n%d %d %d\n" % (n, n, len(el)) +
+        "".join("%d %d\n" % (u + 1, v + 1) for u, v in el))
+    lower = np.stack([el.max(1), el.min(1)], 1)
+    put("er_sym.mtx", "%%%%MatrixMarket matrix coordinate real symmetric\n%d %d %d\n"
+        % (n, n, len(lower)) + "".join("%d %d %.3f\n" % (u + 1, v + 1, x / 7.0)
+                                        for (u, v), x in zip(lower, w)))
+    # METIS: each undirected edge on both endpoints' lines, 1-based, no self-loops
+    adj = [set() for _ in range(n)]
+    for u, v in el:
+        if u != v:
+            adj[u].add(v)
+            adj[v].add(u)
+    # Every adjacency line ends in a space: the reference's METIS reader
+    # (gapbs-verify/reader.h:128-131) drops a line's last entry when no
+    # whitespace follows it, and these files are meant to be read whole.
+    lines = ["% seeded random graph", "%d %d" % (n, sum(len(a) for a in adj) // 2)]
+    for u in range(n):
+        order = sorted(adj[u], key=lambda x: (x * 7919) % n)
+        lines.append("".join("%d " % (v + 1) for v in order))
+        if u == 17:
+            lines.append("% a comment between two vertices")
+    put("er.graph", "\n".join(lines) + "\n")
+    # METIS with edge weights (fmt 1): "neighbour weight" pairs
+    lines = ["%d %d 1" % (n, sum(len(a) for a in adj) // 2)]
+    for u in range(n):
+        lines.append("".join("%d %d " % (v + 1, 1 + (u * v) % 9) for v in sorted(adj[u])))
+    put("er_w.graph", "\n".join(lines) + "\n")
+    # a serialized graph written by this library: the Kronecker-10 graph
+    from dist_mem_gapbs_gb300 import _build, gbbfs
+    _build.build()
+    off, nbr = gbbfs.make_graph(10, 16, False)
+    gbbfs.write_sg(os.path.join(IO_DIR, "g10.sg"), off, nbr)
+    files["g10.sg"] = None
+    return sorted(files)
+
+
+IO_FLAGS = {".el": ["-s"], ".wel": ["-s"], ".gr": ["-s"], ".graph": [], ".sg": []}
+
+
+def main_io():
+    obuild.build_ref()
+    if not O.ref_available():
+        raise SystemExit("reference sources not present: cannot regenerate fixtures")
+    out = {}
+    for name in write_io_inputs():
+        suffix = os.path.splitext(name)[1]
+        flags = ["-f", os.path.join(IO_DIR, name)]
+        flags += ["-s"] if name == "er_general.mtx" else IO_FLAGS.get(suffix, [])
+        with tempfile.TemporaryDirectory() as d:
+            off, nbr = O.ref_graph(flags, d)
+        out[name] = dict(symmetrize="-s" in flags, num_nodes=int(len(off) - 1),
+                         num_edges_directed=int(len(nbr)), offsets_sha256=sha(off),
+                         neigh_sha256=sha(nbr))
+        print(name, out[name]["num_nodes"], out[name]["num_edges_directed"])
+    with open(os.path.join(HERE, "golden_io.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
-    if "--large" in sys.argv:
+    if "--bc" in sys.argv:
+        main_bc()
+    elif "--io" in sys.argv:
+        main_io()
+    elif "--large" in sys.argv:
         main_large([a for a in sys.argv[1:] if not a.startswith("--")])
     else:
         main()

@@ -1,9 +1,16 @@
 """BC's BFS phase on the GPU (gbbfs_bc_bfs) against the oracle's serial
 restatement (gapbs-verify/bc.cc:51-92): path counts, depths and the
 successor bitmap bit for bit, the same level boundaries and the same vertex
-set in every level."""
+set in every level.  And against the reference's PBFS itself: the digests it
+recorded in tests/golden/golden_bc.json."""
+import json
+import os
+
 import numpy as np
 import pytest
+
+from conftest import GOLDEN_DIR, config_args
+from test_reference_pins import bc_digest
 
 pytestmark = pytest.mark.gpu
 
@@ -98,3 +105,19 @@ def test_bc_cli(native, capsys):
     out = capsys.readouterr().out
     assert out.count("source: ") == 3 and "Brandes over 3 sources" in out
     assert out.strip().splitlines()[-5].endswith(":1")      # the top score is the maximum
+
+
+def test_reference_pbfs_fixture(native):
+    """Depths, path counts, successor bits and level sizes equal those of the
+    reference's own PBFS for every recorded source."""
+    with open(os.path.join(GOLDEN_DIR, "golden_bc.json")) as f:
+        fx = json.load(f)
+    for name, gd in sorted(fx.items()):
+        off, nbr = native.make_graph(*config_args(gd["flags"]))
+        with native.Graph(off, nbr) as g:
+            for t in gd["trials"]:
+                sig, dep, succ, order, starts = native.bc_bfs(g, t["source"])
+                d = bc_digest(sig, dep, succ, starts, g.m)
+                for k in ("depth_sha256", "path_counts_sha256", "succ_bits_sha256",
+                          "level_sizes", "reached"):
+                    assert d[k] == t[k], (name, t["source"], k)
