@@ -228,10 +228,74 @@ def cpu_port_sample(off, nbr, sources, budget_s, threads):
     return edges, secs
 
 
+def reference_binary():
+    """oracle/_ref/gapbs_ref when it was compiled on this host from the
+    reference's own gapbs-verify/bfs.cc (and runs here), else None."""
+    from oracle import build as obuild
+    exe = os.path.join(obuild.REF_OUT, "gapbs_ref")
+    if not os.path.exists(exe):
+        return None
+    try:
+        subprocess.run([exe], capture_output=True, timeout=30)
+    except (OSError, subprocess.SubprocessError):
+        return None
+    return exe
+
+
+def run_reference_binary(args, exe):
+    """The reference's own DOBFS (gapbs-verify/bfs.cc:122-173), built from its
+    sources, on every host core: one process builds the graph with the
+    reference's Builder, then times (W + K) x per-step searches cycling over the
+    workload's SourcePicker picks (oracle/ref_driver.cc, time mode)."""
+    scale, degree, uniform = GRAPHS[args.graph]
+    threads = os.cpu_count() or 1
+    per_step = max(1, min(args.sources, 16 if scale >= 25 else args.sources))
+    flags = ["-u" if uniform else "-g", str(scale), "-k", str(degree),
+             "-n", str((args.warmup + args.steps) * per_step)]
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    t0 = time.time()
+    r = subprocess.run([exe, "time", str(args.sources)] + flags, capture_output=True,
+                       text=True, env=env, check=True)
+    wall = time.time() - t0
+    n = m = None
+    trials = []
+    for line in r.stdout.splitlines():
+        f = line.split()
+        if line.startswith("Graph has"):
+            n, m = int(f[2]), 2 * int(f[5])
+        elif f and f[0] == "trial":
+            trials.append((int(f[1]), float(f[2]), int(f[3])))
+    timed = trials[args.warmup * per_step:]
+    edges = [e for _, _, e in timed]
+    secs = [t for _, t, _ in timed]
+    value = hmean_gteps(edges, secs)
+    step_ms = [1e3 * sum(secs[k * per_step:(k + 1) * per_step]) for k in range(args.steps)]
+    sample = ("%d of the %d SourcePicker sources per step (cycling) on %s; gapbs-verify DOBFS "
+              "compiled from the reference's sources (g++ -O3 -fopenmp), %d threads; "
+              "process wall %.0f s incl. the reference's graph build" %
+              (per_step, args.sources, args.graph, threads, wall))
+    line = {
+        "impl": "reference", "metric": "GTEPS (harmonic mean over sources)", "value": value,
+        "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sum(step_ms) / len(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": workload_config(args, n, m),
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "reference",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
+    exe = reference_binary()
+    if exe is not None:
+        return run_reference_binary(args, exe)
     from oracle import oracle as O
     scale, degree, uniform = GRAPHS[args.graph]
     off, nbr = O.build_synthetic(scale, degree, uniform)

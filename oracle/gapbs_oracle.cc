@@ -24,6 +24,8 @@
 
 #include <omp.h>
 
+#include <type_traits>
+
 namespace {
 
 // gapbs-verify/util.h:19 (src/util.h:25)
@@ -246,31 +248,55 @@ int orc_dobfs(const int64_t* off, const int32_t* nbr, int64_t n, int32_t source,
         std::fill(curr.begin(), curr.end(), 0);
         int64_t awake = 0, scanned = 0;
         int64_t unvisited = n - visited;
-        #pragma omp parallel for num_threads(threads) schedule(dynamic, 1024) \
-            reduction(+ : awake, scanned)
-        for (int64_t u = 0; u < n; u++) {
-          if (parent[u] < 0) {
-            for (int64_t e = off[u]; e < off[u + 1]; e++) {
-              int32_t v = nbr[e];
-              scanned++;
-              if ((front[v >> 6] >> (v & 63)) & 1) {
-                parent[u] = v;
-                awake++;
-                __atomic_fetch_or(&curr[u >> 6], uint64_t(1) << (u & 63), __ATOMIC_RELAXED);
-                break;
+        // The scanned-edge count of the byte model is kept only when the
+        // caller asks for step records, so the timed form runs the
+        // reference's loop as it is.
+        auto bu_step = [&](auto counting) {
+          #pragma omp parallel for num_threads(threads) schedule(dynamic, 1024) \
+              reduction(+ : awake, scanned)
+          for (int64_t u = 0; u < n; u++) {
+            if (parent[u] < 0) {
+              for (int64_t e = off[u]; e < off[u + 1]; e++) {
+                int32_t v = nbr[e];
+                if (decltype(counting)::value) scanned++;
+                if ((front[v >> 6] >> (v & 63)) & 1) {
+                  parent[u] = v;
+                  awake++;
+                  __atomic_fetch_or(&curr[u >> 6], uint64_t(1) << (u & 63), __ATOMIC_RELAXED);
+                  break;
+                }
               }
             }
           }
-        }
+        };
+        if (steps)
+          bu_step(std::true_type());
+        else
+          bu_step(std::false_type());
         awake_count = awake;
         visited += awake;
         front.swap(curr);
         rec(ORC_BU, awake_count, old_awake_count, scanned, awake, unvisited);
       } while ((awake_count >= old_awake_count) || (awake_count > n / beta));
-      // BitmapToQueue (bitmap order; the reference fills per-thread buffers,
-      // so its queue order is not fixed either)
-      for (int64_t u = 0; u < n; u++)
-        if ((front[u >> 6] >> (u & 63)) & 1) queue[q_in++] = (int32_t)u;
+      // BitmapToQueue: per-thread buffers appended at an atomic tail, as the
+      // reference's QueueBuffer does (so the queue order is not fixed; one
+      // thread gives bitmap order).
+      {
+        std::atomic<int64_t> tail(q_in);
+        #pragma omp parallel num_threads(threads)
+        {
+          std::vector<int32_t> local;
+          local.reserve(4096);
+          #pragma omp for schedule(static) nowait
+          for (int64_t w = 0; w < words; w++) {
+            for (uint64_t x = front[w]; x; x &= x - 1)
+              local.push_back((int32_t)(64 * w + __builtin_ctzll(x)));
+          }
+          int64_t at = tail.fetch_add((int64_t)local.size());
+          std::copy(local.begin(), local.end(), queue.begin() + at);
+        }
+        q_in = tail.load();
+      }
       q_begin = q_end; q_end = q_in;
       std::fill(front.begin(), front.end(), 0);
       rec(ORC_C, 0, 0, 0, q_end - q_begin, 0);
@@ -280,6 +306,8 @@ int orc_dobfs(const int64_t* off, const int32_t* nbr, int64_t n, int32_t source,
       edges_to_check -= scout_count;
       int64_t fsize = q_end - q_begin, examined = 0, scout = 0;
       std::atomic<int64_t> tail(q_in);
+      // The examined-edge count equals the frontier's degree sum; it is
+      // summed per vertex, outside the edge loop.
       #pragma omp parallel num_threads(threads) reduction(+ : examined, scout)
       {
         std::vector<int32_t> local;
@@ -287,9 +315,9 @@ int orc_dobfs(const int64_t* off, const int32_t* nbr, int64_t n, int32_t source,
         #pragma omp for schedule(dynamic, 64)
         for (int64_t i = q_begin; i < q_end; i++) {
           int32_t u = queue[i];
+          examined += off[u + 1] - off[u];
           for (int64_t e = off[u]; e < off[u + 1]; e++) {
             int32_t v = nbr[e];
-            examined++;
             int32_t curr_val = __atomic_load_n(&parent[v], __ATOMIC_RELAXED);
             if (curr_val < 0) {
               if (__atomic_compare_exchange_n(&parent[v], &curr_val, u, false,

@@ -14,7 +14,9 @@
 //             reference's own PrintStep trace; parents of all trials are appended
 //             to <prefix>.par (int32[n] per trial)
 //   time    : time DOBFS for -n trials (as src/benchmark.h:127-129 brackets it) and
-//             print one "trial <source> <seconds> <reached_degree_sum>" line each
+//             print one "trial <source> <seconds> <reached_degree_sum>" line each;
+//             here <out-prefix> is a count c: the trials cycle over the first c
+//             SourcePicker picks (0: a fresh pick per trial)
 //   fixture : one graph build, then everything a golden fixture records, without
 //             writing the (multi-GB) arrays out:
 //               "graph <n> <m_dir> <sha256 offsets int64> <sha256 neigh int32>"
@@ -27,6 +29,7 @@
 #undef main
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <string>
@@ -103,8 +106,13 @@ int main(int argc, char* argv[]) {
     return 0;
   }
   if (mode == "time") {
+    // The out-prefix argument names how many SourcePicker picks the trials
+    // cycle over (0: a fresh pick per trial).
+    const int cycle = atoi(prefix.c_str());
+    std::vector<NodeID> picks;
+    for (int i = 0; i < cycle; i++) picks.push_back(sp.PickNext());
     for (int i = 0; i < cli.num_trials(); i++) {
-      NodeID s = sp.PickNext();
+      NodeID s = cycle > 0 ? picks[i % cycle] : sp.PickNext();
       Timer t;
       t.Start();
       pvector<NodeID> parent = DOBFS(g, s);
