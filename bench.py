@@ -542,6 +542,35 @@ def run_bc(gbbfs, g, sources, deg):
             "brandes_ms_per_source": brandes_ms}
 
 
+def check_batched_rows(gbbfs, g, batched, lanes):
+    """Outside the timed region: every batch run again with its rows left in
+    HBM, each row digested on the device (sum over v of (d[v] + 1) * (v + 1) *
+    0x9E3779B97F4A7C15 mod 2^64, d = 255 where unreached), and compared with
+    the same digest of the single-source search from that row's source."""
+    import torch
+    n = g.n
+    k64 = 0x9E3779B97F4A7C15 - (1 << 64)
+    w = torch.arange(1, n + 1, dtype=torch.int64, device="cuda") * k64
+
+    def digest(d):                       # d: int64 depth with 255 for unreached
+        return int(((d + 1) * w).sum().item())
+
+    ok = checked = 0
+    for b in range(0, len(batched), lanes):
+        srcs = batched[b:b + lanes]
+        ptr, _ = gbbfs.msbfs_device(g, srcs, 1)
+        rows = torch.as_tensor(gbbfs.DeviceArray(ptr, (len(srcs), n), "|u1"), device="cuda")
+        got = [digest(rows[i].to(torch.int64)) for i in range(len(srcs))]
+        for i, s in enumerate(srcs):
+            gbbfs.bfs_device(g, int(s), want_depth=True)
+            _, dptr = gbbfs.result_device_ptrs(g)
+            d = torch.as_tensor(gbbfs.DeviceArray(dptr, (n,), "<i4"), device="cuda")
+            d = torch.where(d < 0, 255, d).to(torch.int64)
+            checked += 1
+            ok += digest(d) == got[i]
+    return ok, checked
+
+
 def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
     """Batched multi-source BFS on Kronecker-24: queries/s for 4096 sources
     against back-to-back plain single-source launches, rows spot-checked."""
@@ -574,13 +603,19 @@ def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
         fifo_ms = 0.0
         for b in range(0, queries, lanes):
             fifo_ms += gbbfs.msbfs_device(g, srcs[b:b + lanes], 1)[1].device_ms
-        # the last batch's rows against single-source depths
-        last = batched[queries - lanes:queries]
-        rows = gbbfs.msbfs(g, last[:4], 4)
-        for i in range(4):
-            d = gbbfs.DOBFS(g, int(last[i]), depth=True)[1]
-            if not np.array_equal(rows[i], d):
-                raise AssertionError("batched depths differ from the single-source search")
+        rows_ok, rows_checked = check_batched_rows(gbbfs, g, batched, lanes)
+        if rows_ok != rows_checked:
+            raise AssertionError("%d of %d batched depth rows differ from the single-source "
+                                 "search" % (rows_checked - rows_ok, rows_checked))
+        # a few rows against the oracle's serial BFS as well
+        from oracle import oracle as O
+        last = batched[queries - 2:queries]
+        rows = gbbfs.msbfs(g, last, 4)
+        _, nbr_h = g.csr()
+        for i in range(len(last)):
+            if not np.array_equal(rows[i], O.depth(off, nbr_h, int(last[i]))):
+                raise AssertionError("batched depths differ from the oracle")
+        del nbr_h
         # with the depth rows streamed to host memory, batch by batch
         import torch
         pinned = torch.empty((lanes, g.n), dtype=torch.uint8, pin_memory=True).numpy()
@@ -595,7 +630,10 @@ def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
                 "queries_per_s_in_given_order": queries / (fifo_ms * 1e-3),
                 "order_ms": order_ms,
                 "config": best, "autotune_s": tune_s, "device_ms": dev_ms,
-                "td_ms": td_ms, "bu_ms": bu_ms, "rows_checked": 4}
+                "td_ms": td_ms, "bu_ms": bu_ms, "rows_checked": rows_checked,
+                "rows_equal": rows_ok, "oracle_rows_checked": 2,
+                "rows_check": "every row's depth digest (on the device) against the digest of "
+                              "the single-source search from its source"}
 
 
 def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=4096):

@@ -667,21 +667,26 @@ int gbbfs_bfs_many(gbbfs_graph* g, const int32_t* sources, int64_t k, int alpha,
   for (int64_t i = 0; i < k; i++)
     if (!parent_out[i]) return GBBFS_ERR_ARG;
   GB_CUDA(cudaSetDevice(g->device));
-  if (!g->copy_stream) {
-    for (int i = 0; i < 2; i++) {
+  // Made on first use; each resource is checked on its own, so a call after
+  // a failed one completes the set-up instead of making any part twice.
+  for (int i = 0; i < 2; i++) {
+    if (!g->stage[i]) {
       cudaError_t e = cudaMalloc(&g->stage[i], sizeof(int32_t) * 32 * (size_t)g->W);
       if (e != cudaSuccess) {
+        g->stage[i] = nullptr;
         g_last_error = std::string("parent arrays: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? GBBFS_ERR_NOMEM : GBBFS_ERR_CUDA;
       }
       g->device_bytes += (int64_t)sizeof(int32_t) * 32 * g->W;
-      GB_CUDA(cudaEventCreateWithFlags(&g->staged[i], cudaEventDisableTiming));
-      GB_CUDA(cudaEventCreateWithFlags(&g->copied[i], cudaEventDisableTiming));
     }
+    if (!g->staged[i]) GB_CUDA(cudaEventCreateWithFlags(&g->staged[i], cudaEventDisableTiming));
+    if (!g->copied[i]) GB_CUDA(cudaEventCreateWithFlags(&g->copied[i], cudaEventDisableTiming));
+  }
+  if (!g->copy_stream)
     GB_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+  if (!g->h_slot)
     GB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->h_slot), 2 * sizeof(DevState),
                           cudaHostAllocDefault));
-  }
   if (!st) {
     if (alpha <= 0) alpha = 15;
     if (beta <= 0) beta = 18;

@@ -1,15 +1,14 @@
 // gbbfs_bfs_noalloc: one direction-optimizing BFS that allocates nothing.
 //
 // Some callers cannot allocate device memory at the moment they need a
-// search: code that runs while a CUDA stream is being captured into a graph
-// (an allocation there is either refused or breaks the capture), plugins
-// that live inside a framework whose own caching allocator owns the device
-// and must not be bypassed, and latency-bound loops that cannot afford the
-// device-wide synchronisation cudaMalloc / cudaFree may cause.  For them this
-// entry point takes the graph and the result buffers as device pointers the
-// caller already owns, and keeps every intermediate it needs (frontier
-// bitmaps, queues, counters, control state) in one fixed array of device
-// memory that is part of the library itself.
+// search: plugins that live inside a framework whose own caching allocator
+// owns the device (memory taken behind its back is memory it cannot account
+// for or reuse), and loops that cannot afford the device-wide
+// synchronisation cudaMalloc / cudaFree may cause.  For them this entry point
+// takes the graph and the result buffers as device pointers the caller
+// already owns, and keeps every intermediate it needs (frontier bitmaps,
+// queues, counters, control state) in one fixed array of device memory that
+// is part of the library itself.
 //
 // The array is a file-scope __device__ variable of kNoAllocScratchBytes
 // (about 8.2 MB), sized for graphs of at most kNoAllocMaxVertices vertices.
@@ -21,8 +20,14 @@
 // Host code cannot pass the array's name to a kernel: on the host that name
 // is only a stand-in, not a device address.  The first call on each device
 // therefore looks the address up with cudaGetSymbolAddress while that device
-// is current, and caches it; that first call should happen before any
-// stream capture begins.
+// is current, and caches it with the launch grids of the step kernels.  The
+// cache assumes the device's primary context lives as long as the process
+// (no cudaDeviceReset between calls).
+//
+// The search is stepped from the host: after each step the host reads the
+// device's choice of the next one and synchronises the stream.  So the call
+// must not be made on a stream that is being captured into a CUDA graph; it
+// checks, and returns GBBFS_ERR_STATE without touching the stream.
 
 #include <cuda_runtime.h>
 
@@ -60,26 +65,15 @@ constexpr size_t kNoAllocScratchBytes = kOffQs1 + align256(8 * kNoAllocMaxVertic
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (looked up once).
-int scratch_address(unsigned char** out) {
-  int dev = 0;
-  GB_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    last_error() = "device index beyond the scratch table";
-    return GBBFS_ERR_ARG;
-  }
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    GB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-  }
-  *out = g_scratch_ptr[dev];
-  return GBBFS_OK;
-}
+// Per device: the scratch array's address and the grids of the step kernels.
+struct DeviceSetup {
+  unsigned char* scratch = nullptr;
+  int sms = 0;
+  int g_init = 0, g_td = 0, g_bu = 0, g_q2b = 0, g_b2q = 0, g_tdb = 0;
+};
+std::mutex g_setup_mu;
+DeviceSetup g_setup[kMaxDevices];
 
 int bits(uint64_t x) {
   int b = 0;
@@ -94,6 +88,37 @@ int occupancy(const void* fn, int sms, int* grid) {
   int per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
   *grid = (per_sm > 0 ? per_sm : 1) * sms;
+  return GBBFS_OK;
+}
+
+// Set-up of the current device, done once: the device address of the
+// scratch array (cudaGetSymbolAddress, with that device current) and the
+// launch grids.
+int device_setup(const DeviceSetup** out) {
+  typedef unsigned long long OffT;
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    last_error() = "device index beyond the scratch table";
+    return GBBFS_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  DeviceSetup& d = g_setup[dev];
+  if (!d.scratch) {
+    DeviceSetup t;
+    void* p = nullptr;
+    GB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    t.scratch = static_cast<unsigned char*>(p);
+    GB_CUDA(cudaDeviceGetAttribute(&t.sms, cudaDevAttrMultiProcessorCount, dev));
+    GB_TRY(occupancy((const void*)k_init<OffT>, t.sms, &t.g_init));
+    GB_TRY(occupancy((const void*)k_td<OffT>, t.sms, &t.g_td));
+    GB_TRY(occupancy((const void*)k_bu<OffT, 0>, t.sms, &t.g_bu));
+    GB_TRY(occupancy((const void*)k_q2b<OffT>, t.sms, &t.g_q2b));
+    GB_TRY(occupancy((const void*)k_b2q<OffT, false>, t.sms, &t.g_b2q));
+    GB_TRY(occupancy((const void*)k_tdb<OffT>, t.sms, &t.g_tdb));
+    d = t;
+  }
+  *out = &d;
   return GBBFS_OK;
 }
 
@@ -128,12 +153,20 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   if (alpha <= 0) alpha = 15;
   if (beta <= 0) beta = 18;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  GB_CUDA(cudaStreamIsCapturing(s, &capturing));
+  if (capturing != cudaStreamCaptureStatusNone) {
+    last_error() = "gbbfs_bfs_noalloc synchronises its stream after every step and cannot "
+                   "run on a stream that is being captured";
+    return GBBFS_ERR_STATE;
+  }
 
-  unsigned char* base = nullptr;
-  GB_TRY(scratch_address(&base));
-  int dev = 0, sms = 0;
-  GB_CUDA(cudaGetDevice(&dev));
-  GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const DeviceSetup* d = nullptr;
+  GB_TRY(device_setup(&d));
+  unsigned char* base = d->scratch;
+  const int sms = d->sms;
+  const int g_init = d->g_init, g_td = d->g_td, g_bu = d->g_bu, g_q2b = d->g_q2b,
+            g_b2q = d->g_b2q, g_tdb = d->g_tdb;
 
   Bufs<OffT> b;
   b.off = reinterpret_cast<const OffT*>(d_offsets);
@@ -154,14 +187,6 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   b.m = m_dir;
   b.W = (n + 31) / 32;
   b.shift = shift;
-
-  int g_init = 0, g_td = 0, g_bu = 0, g_q2b = 0, g_b2q = 0, g_tdb = 0;
-  GB_TRY(occupancy((const void*)k_init<OffT>, sms, &g_init));
-  GB_TRY(occupancy((const void*)k_td<OffT>, sms, &g_td));
-  GB_TRY(occupancy((const void*)k_bu<OffT, 0>, sms, &g_bu));
-  GB_TRY(occupancy((const void*)k_q2b<OffT>, sms, &g_q2b));
-  GB_TRY(occupancy((const void*)k_b2q<OffT, false>, sms, &g_b2q));
-  GB_TRY(occupancy((const void*)k_tdb<OffT>, sms, &g_tdb));
 
   // Start from a clean control block (the previous call left its own state),
   // with the timer stamps at their neutral values.

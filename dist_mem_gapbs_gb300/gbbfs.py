@@ -462,6 +462,25 @@ def results(g, parent_out=None, depth_out=None):
     _check(lib().gbbfs_results(g.handle, _p(parent_out), _p(depth_out)), "results")
 
 
+def result_device_ptrs(g):
+    """Device addresses (parent, depth) of the handle's last search; depth is
+    None unless that search kept depths."""
+    pp, dp = ctypes.c_void_p(), ctypes.c_void_p()
+    _check(lib().gbbfs_result_device_ptrs(g.handle, ctypes.byref(pp), ctypes.byref(dp)),
+           "result_device_ptrs")
+    return pp.value, dp.value
+
+
+class DeviceArray:
+    """A device buffer of this library seen through __cuda_array_interface__
+    (so torch.as_tensor(..., device="cuda") can read it without a copy)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
+                                         "data": (int(ptr), False), "version": 3,
+                                         "strides": None}
+
+
 def write_bfs_output(path, parent):
     p = np.ascontiguousarray(parent, dtype=np.int32)
     _check(lib().gbbfs_append_bfs_output(os.fsencode(path), _p(p), len(p)), "append_bfs_output")

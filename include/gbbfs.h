@@ -130,9 +130,9 @@ int gbbfs_bfs_device(gbbfs_graph* g, int32_t source, int alpha, int beta,
                      int want_depth, gbbfs_stats* st);
 
 /* The same search for callers that cannot allocate device memory when they
- * need it: code running while a stream is being captured into a CUDA graph,
- * plugins inside a framework whose own allocator owns the device, loops that
- * cannot afford the synchronisation cudaMalloc / cudaFree may cause.  No
+ * need it: plugins inside a framework whose own allocator owns the device
+ * (memory taken behind its back is memory it cannot account for), and loops
+ * that cannot afford the synchronisation cudaMalloc / cudaFree may cause.  No
  * counterpart in the reference.  Everything is caller-owned device memory:
  * d_offsets int64[n+1], d_neigh int32[m_dir] (symmetric CSR), d_parent_out
  * int32[n] (same encoding as gbbfs_bfs), d_depth_out int32[n] or NULL; stream
@@ -141,9 +141,12 @@ int gbbfs_bfs_device(gbbfs_graph* g, int32_t source, int alpha, int beta,
  * is part of the library (about 8.2 MB, held on every GPU that loads the
  * library until exit), so graphs are limited to n <= 262144 vertices
  * (GBBFS_ERR_ARG beyond).  Nothing is allocated, by this call or the
- * library.  The first call on a device looks up that array's address; make
- * it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller. */
+ * library.  The first call on a device looks up that array's address (and
+ * the kernels' launch grids) once.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  The search
+ * is stepped from the host, with a stream synchronisation after every step,
+ * so the stream must not be one that is being captured into a CUDA graph
+ * (GBBFS_ERR_STATE, the stream untouched). */
 int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t n,
                       int64_t m_dir, int32_t source, int alpha, int beta,
                       int32_t* d_parent_out, int32_t* d_depth_out, void* stream);

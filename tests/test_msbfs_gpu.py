@@ -129,3 +129,34 @@ def test_msbfs_order(native, batch_keys):
         native.msbfs_set_config(g, 32, 8, 15)
         ref = single_depths(native, g, srcs[:80])
         assert np.array_equal(native.msbfs(g, srcs[:80], 4), ref)
+
+
+def test_msbfs_rows_equal_reference_fixture(native, golden):
+    """Every row of a batch over the reference's recorded sources hashes to the
+    depth array the reference's DOBFS implies (golden.json, Kronecker-18; and
+    golden_large.json, Kronecker-22 with all 64 sources)."""
+    import hashlib
+    import json
+    import os
+    from conftest import GOLDEN_DIR, config_args
+    with open(os.path.join(GOLDEN_DIR, "golden_large.json")) as f:
+        large = json.load(f)
+    for gd in (golden["g18"], large["g22"]):
+        srcs = np.array([t["source"] for t in gd["trials"]], np.int32)
+        el = native.generate_edges(*config_args(gd["flags"]))
+        with native.Graph.from_edges(el) as g:
+            rows = native.msbfs(g, srcs, 1)
+            for row, t in zip(rows, gd["trials"]):
+                d = as_int32(row)
+                assert hashlib.sha256(d.tobytes()).hexdigest() == t["depth_sha256"], t["source"]
+
+
+def test_msbfs_rows_equal_oracle(native, oracle):
+    """16 rows of a 256-lane batch against the oracle's serial BFS depths."""
+    off, nbr = native.make_graph(17, 16, False)
+    with native.Graph(off, nbr) as g:
+        native.msbfs_set_config(g, 256, 8, 15)
+        srcs = native.pick_sources(off, 256)
+        rows = native.msbfs(g, srcs, 4)
+        for i in range(0, 256, 16):
+            assert np.array_equal(rows[i], oracle.depth(off, nbr, int(srcs[i]))), i

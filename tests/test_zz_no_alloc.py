@@ -49,6 +49,7 @@ def test_noalloc_matches_gbbfs_bfs(native, oracle, golden, name):
             p_new, d_new = _noalloc(native, torch, d_off, d_nbr, n, m, src)
             p_ref, d_ref = native.DOBFS(g, src, depth=True)
             assert np.array_equal(d_new, d_ref)
+            assert np.array_equal(d_new, oracle.depth(off, nbr, src))
             assert oracle.verify(off, nbr, src, p_new)[0]
             assert oracle.verify(off, nbr, src, p_ref)[0]
             assert p_new[src] == src
@@ -88,3 +89,64 @@ def test_noalloc_rejects_oversize_and_bad_source(native):
     rc = L.gbbfs_bfs_noalloc(*args, len(off) - 1, len(nbr), len(off) + 4, 15, 18,
                              ctypes.c_void_p(parent.data_ptr()), None, None)
     assert rc == native.ERR_ARG
+
+
+def _driver():
+    """The CUDA driver library, for stream capture without any other package."""
+    for name in ("libcuda.so.1", "libcuda.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            pass
+    pytest.skip("libcuda not found")
+
+
+def test_noalloc_allocates_nothing(native, oracle):
+    """Device free memory is the same before and after a call (the kernels it
+    launches were loaded by the same call just before)."""
+    torch = pytest.importorskip("torch")
+    off, nbr = native.make_graph(14, 16, False)
+    n, m = len(off) - 1, len(nbr)
+    d_off, d_nbr = _device_csr(torch, off, nbr)
+    src = int(native.pick_sources(off, 1)[0])
+    _noalloc(native, torch, d_off, d_nbr, n, m, src)
+    _noalloc(native, torch, d_off, d_nbr, n, m, src)
+    parent = torch.empty(n, dtype=torch.int32, device="cuda")
+    depth = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    rc = native.lib().gbbfs_bfs_noalloc(
+        ctypes.c_void_p(d_off.data_ptr()), ctypes.c_void_p(d_nbr.data_ptr()), n, m, src, 15, 18,
+        ctypes.c_void_p(parent.data_ptr()), ctypes.c_void_p(depth.data_ptr()), None)
+    assert rc == native.OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert np.array_equal(depth.cpu().numpy(), oracle.depth(off, nbr, src))
+
+
+def test_noalloc_refuses_a_capturing_stream(native):
+    """The call synchronises its stream after every step, so on a stream under
+    capture it must return GBBFS_ERR_STATE and leave the capture untouched."""
+    torch = pytest.importorskip("torch")
+    off, nbr = native.make_graph(10, 16, True)
+    n, m = len(off) - 1, len(nbr)
+    d_off, d_nbr = _device_csr(torch, off, nbr)
+    parent = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    cu = _driver()
+    stream, graph = ctypes.c_void_p(), ctypes.c_void_p()
+    assert cu.cuStreamCreate(ctypes.byref(stream), 1) == 0          # non-blocking
+    try:
+        assert cu.cuStreamBeginCapture_v2(stream, 1) == 0           # thread-local mode
+        rc = native.lib().gbbfs_bfs_noalloc(
+            ctypes.c_void_p(d_off.data_ptr()), ctypes.c_void_p(d_nbr.data_ptr()), n, m, 0,
+            15, 18, ctypes.c_void_p(parent.data_ptr()), None, stream)
+        err = native.lib().gbbfs_last_error()
+        assert cu.cuStreamEndCapture(stream, ctypes.byref(graph)) == 0   # still valid
+        assert rc == native.ERR_STATE and b"captured" in err
+        nodes = ctypes.c_size_t(99)
+        assert cu.cuGraphGetNodes(graph, None, ctypes.byref(nodes)) == 0
+        assert nodes.value == 0                                     # nothing was enqueued
+        cu.cuGraphDestroy(graph)
+    finally:
+        cu.cuStreamDestroy_v2(stream)
