@@ -636,7 +636,24 @@ def run_batched(gbbfs, scale=24, queries=4096, plain_sample=256):
                               "the single-source search from its source"}
 
 
-def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=4096):
+def batch_overlap(results):
+    """Share of the time some batch kernel ran during which two or more did
+    (from the batch kernels' own device-clock stamps in the results)."""
+    iv = sorted({(r["device_begin_ns"], r["device_end_ns"]) for r in results
+                 if r["device_begin_ns"]})
+    ev = sorted([(a, 1) for a, _ in iv] + [(b, -1) for _, b in iv])
+    cur, last, busy, multi = 0, None, 0, 0
+    for t, d in ev:
+        if last is not None and cur > 0:
+            busy += t - last
+            if cur > 1:
+                multi += t - last
+        cur += d
+        last = t
+    return multi / busy if busy else 0.0
+
+
+def run_serving(gbbfs, rates=(1000, 5000, 10000, 20000), duration_s=2.0, burst=4096):
     """Query server over the 8-graph pool: saturation throughput batched vs
     plain per-query launches, and p50/p99 latency under Poisson arrivals."""
     from dist_mem_gapbs_gb300 import serving
@@ -679,9 +696,31 @@ def run_serving(gbbfs, rates=(2000, 10000), duration_s=3.0, burst=4096):
                     out["latency"] = []
                     for rate in rates:
                         r = serving.run_open_loop(srv, sources, rate, duration_s)
-                        r.pop("results")
+                        res = r.pop("results")
+                        r["batch_overlap"] = batch_overlap(res)
+                        r["p50_ms_by_graph"] = [
+                            float(np.percentile([x["done_s"] - x["submit_s"] for x in res
+                                                 if x["graph_id"] == gid], 50) * 1e3)
+                            for gid in range(len(graphs))]
                         out["latency"].append(r)
         out["ratio_vs_plain"] = out["batched_saturation_qps"] / out["plain_saturation_qps"]
+        out["saturation_vs_50k_offered"] = out["batched_saturation_qps"] / 50000.0
+        out["policy"] = "every batch spans the whole GPU, one batch per graph in flight"
+        # The same pool with the SMs split among the graphs (grid_policy 1):
+        # batches of different graphs run side by side.
+        with gbbfs.Server(mode=gbbfs.Server.BATCHED, grid_policy=1) as srv:
+            for g in graphs:
+                srv.add_graph(g)
+            for gid in range(len(graphs)):
+                srv.submit(gid, sources[gid][0])
+            srv.drain()
+            srv.poll(4096)
+            out["split_sms_latency"] = []
+            for rate in rates[1:3]:
+                r = serving.run_open_loop(srv, sources, rate, duration_s)
+                res = r.pop("results")
+                r["batch_overlap"] = batch_overlap(res)
+                out["split_sms_latency"].append(r)
     finally:
         for g in graphs:
             g.close()

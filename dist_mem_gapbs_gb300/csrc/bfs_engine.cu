@@ -553,6 +553,16 @@ int bfs_enqueue(gbbfs_graph* g, int32_t source, void* h_params) {
 
 const int32_t* bfs_depth(const gbbfs_graph* g) { return g->depth; }
 
+int graph_set_stream_priority(gbbfs_graph* g, int priority) {
+  GB_CUDA(cudaSetDevice(g->device));
+  GB_CUDA(cudaStreamSynchronize(g->stream));
+  cudaStream_t s = nullptr;
+  GB_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, priority));
+  cudaStreamDestroy(g->stream);
+  g->stream = s;
+  return GBBFS_OK;
+}
+
 const int32_t* bfs_error_word(const gbbfs_graph* g) { return &g->st->error; }
 
 // A handle from a CSR already in device memory (offsets int64[n+1],

@@ -37,6 +37,9 @@ namespace gbbfs {
 size_t ms_state_bytes(int64_t n, int64_t m, int64_t W, int depth_bytes);  // HBM a handle's state takes
 int ms_prepare(gbbfs_graph* g, int depth_bytes);   // allocate (or keep) the state
 int ms_lanes(const gbbfs_graph* g);
+// SMs a batch's cooperative grid spans on this handle (0: all of them); the
+// handle's captured batch graphs are remade at their next launch.
+int ms_set_grid_sms(gbbfs_graph* g, int sms);
 int ms_launch(gbbfs_graph* g, int buf, const int32_t* sources, int k);
 bool ms_ready(gbbfs_graph* g, int buf);            // batch in `buf` has finished
 int ms_finish(gbbfs_graph* g, int buf);            // wait, then report its status
@@ -47,6 +50,8 @@ void ms_mark_copied(gbbfs_graph* g, int buf, cudaStream_t s);  // copies out of 
 // its own start and end stamps (a cooperative kernel runs alone once started,
 // so this excludes waits for other work).
 double ms_kernel_ms(const gbbfs_graph* g, int buf);
+// Device clock (%globaltimer, ns) at that kernel's start and end.
+void ms_kernel_stamps(const gbbfs_graph* g, int buf, uint64_t* begin_ns, uint64_t* end_ns);
 // Indices of sources[0..k) in the order to batch them (gbbfs_msbfs_order).
 int ms_order(gbbfs_graph* g, const int32_t* sources, int64_t k, int32_t* order);
 
@@ -65,6 +70,9 @@ int radix_sort64(uint64_t* keys, uint64_t* tmp, int64_t len, int key_bits, cudaS
 constexpr size_t kSearchParamBytes = offsetof(DevState, edges_to_check);
 int bfs_enqueue(gbbfs_graph* g, int32_t source, void* h_params);
 const int32_t* bfs_depth(const gbbfs_graph* g);
+// Replace the handle's stream by one of the given priority (lower numbers
+// run first, cudaDeviceGetStreamPriorityRange); waits for the old stream.
+int graph_set_stream_priority(gbbfs_graph* g, int priority);
 const int32_t* bfs_error_word(const gbbfs_graph* g);
 
 // A handle from a CSR in device memory (bfs_engine.cu): offsets int64[n+1]

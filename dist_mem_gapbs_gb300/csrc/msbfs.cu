@@ -77,7 +77,11 @@ struct MsState {
   // size.
   cudaGraphExec_t exec[2][kLaneClasses] = {};
   MsConfig exec_cfg[2][kLaneClasses];
+  int exec_sms[2][kLaneClasses] = {};
   MsConfig cfg;
+  // SMs the persistent kernel's grid spans (0: all).  A query server gives
+  // each graph a share, so batches of several graphs run on the GPU at once.
+  int grid_sms = 0;
   int64_t bytes = 0;
   int last_buf = -1;
   int last_k = 0;
@@ -471,6 +475,12 @@ int ensure_state(gbbfs_graph* g, int depth_bytes) {
   return GBBFS_OK;
 }
 
+// SMs a batch's grid spans on this handle.
+int grid_sms(const gbbfs_graph* g) {
+  const int share = g->ms ? g->ms->grid_sms : 0;
+  return share > 0 && share < g->sms ? share : g->sms;
+}
+
 template <typename OffT, typename LaneT, typename DepthT>
 int capture_batch(gbbfs_graph* g, int buf, int cls) {
   MsState* ms = g->ms;
@@ -483,7 +493,7 @@ int capture_batch(gbbfs_graph* g, int buf, int cls) {
     ms_error = "multi-source kernel does not fit on an SM";
     return GBBFS_ERR_CUDA;
   }
-  const int grid = per_sm * g->sms;
+  const int grid = per_sm * grid_sms(g);
   MsArgs<OffT, LaneT, DepthT> a;
   a.off = reinterpret_cast<const OffT*>(ms->roff);
   a.nbr = ms->rnbr;
@@ -573,6 +583,7 @@ int capture_batch(gbbfs_graph* g, int buf, int cls) {
     return GBBFS_ERR_CUDA;
   }
   ms->exec_cfg[buf][cls] = cfg;
+  ms->exec_sms[buf][cls] = grid_sms(g);
   return GBBFS_OK;
 }
 
@@ -604,7 +615,9 @@ int capture_all(gbbfs_graph* g) {
     for (int cls = 0; (32 << cls) <= ms->cfg.lanes; cls++) {
       MsConfig want = ms->cfg;
       want.lanes = 32 << cls;
-      if (ms->exec[buf][cls] && same_cfg(ms->exec_cfg[buf][cls], want)) continue;
+      if (ms->exec[buf][cls] && same_cfg(ms->exec_cfg[buf][cls], want) &&
+          ms->exec_sms[buf][cls] == grid_sms(g))
+        continue;
       if (!synced) {
         GB_CUDA(cudaStreamSynchronize(g->stream));
         synced = true;
@@ -632,7 +645,9 @@ int launch_batch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
   want.lanes = 32 << cls;
   // The buffer's previous results must have left the device first.
   GB_CUDA(cudaStreamWaitEvent(g->stream, ms->copied[buf], 0));
-  if (!ms->exec[buf][cls] || !same_cfg(ms->exec_cfg[buf][cls], want)) GB_TRY(capture_all(g));
+  if (!ms->exec[buf][cls] || !same_cfg(ms->exec_cfg[buf][cls], want) ||
+      ms->exec_sms[buf][cls] != grid_sms(g))
+    GB_TRY(capture_all(g));
   // The host copy of the sources is read by the graph's first node; wait
   // until the previous launch that read this slot is done.
   GB_CUDA(cudaEventSynchronize(ms->computed[buf]));
@@ -771,6 +786,12 @@ int ms_prepare(gbbfs_graph* g, int depth_bytes) {
 
 int ms_lanes(const gbbfs_graph* g) { return g->ms ? g->ms->cfg.lanes : MsConfig().lanes; }
 
+int ms_set_grid_sms(gbbfs_graph* g, int sms) {
+  if (!g->ms) return GBBFS_ERR_STATE;
+  g->ms->grid_sms = sms < 0 ? 0 : sms;   // graphs are recaptured on the next launch
+  return GBBFS_OK;
+}
+
 int ms_launch(gbbfs_graph* g, int buf, const int32_t* sources, int k) {
   if (!g->ms || k < 1 || k > g->ms->cfg.lanes) return GBBFS_ERR_STATE;
   return launch_batch(g, buf, sources, k);
@@ -789,6 +810,12 @@ void* ms_depth(gbbfs_graph* g, int buf) { return g->ms->depth[buf]; }
 double ms_kernel_ms(const gbbfs_graph* g, int buf) {
   const MsCtl& c = g->ms->h_ctl[buf];
   return c.t_end > c.t_begin ? (double)(c.t_end - c.t_begin) * 1e-6 : 0.0;
+}
+
+void ms_kernel_stamps(const gbbfs_graph* g, int buf, uint64_t* begin_ns, uint64_t* end_ns) {
+  const MsCtl& c = g->ms->h_ctl[buf];
+  *begin_ns = c.t_begin;
+  *end_ns = c.t_end;
 }
 
 cudaEvent_t ms_done_event(gbbfs_graph* g, int buf) { return g->ms->computed[buf]; }

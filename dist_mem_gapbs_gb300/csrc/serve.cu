@@ -17,7 +17,12 @@
 // take less than one batch and few batches are in flight: the small kernels
 // of a plain search queue behind other graphs' batches, which hold the whole
 // GPU, so under load a batch answers sooner.  Batches of different graphs run
-// on their graphs' own streams and overlap on the device.  The per-graph
+// on their graphs' own streams.  By default each batch's persistent kernel
+// spans the whole GPU and the graphs' batches take turns; grid_policy 1 gives
+// each graph its own share of the SMs (a reserve for the small kernels
+// around batches, at least 8 SMs per graph, the rest by the square root of
+// the graph's measured batch cost), so a small graph's batch runs beside a
+// large graph's instead of waiting for the whole GPU.  The per-graph
 // search state (visit / frontier words, depth rows) is admitted against free
 // HBM and an optional byte budget; an idle graph gives its state back when
 // another graph needs the room.  mode 1 answers every query with its own
@@ -31,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -104,6 +110,7 @@ struct Query {
   double t_submit, t_start, t_done;
   int batch;
   bool plain;
+  uint64_t dev_begin, dev_end;   // the answering batch kernel's device clock stamps
 };
 
 struct Inflight {
@@ -128,6 +135,8 @@ struct Slot {
   // batch per lane width class (running); negative while unmeasured.
   double plain_ms = -1;
   double batch_ms[4] = {-1, -1, -1, -1};
+  double full_batch_ms = -1;     // a 1-source batch on the whole GPU (at admission)
+  int priority = 1 << 30;        // stream priority given (none yet)
 };
 
 constexpr size_t kParBlock = 64;   // bytes per parameter block in h_par
@@ -169,6 +178,69 @@ int64_t state_bytes_in_use(gbbfs_server* s) {
   return b;
 }
 
+// SMs a graph's batches span (0 = the whole GPU).  grid_policy 1 splits the
+// SMs among the admitted graphs so that their batches run side by side: a
+// reserve of kReserveSms is left for the small kernels around the batches
+// (buffer clears, depth decode, digests), which would otherwise wait for a
+// batch to finish; every graph gets kMinShareSms, and the rest goes in
+// proportion to the square root of the graph's measured batch cost on the
+// whole GPU.  (With equal query rates that split minimises the mean batch
+// time when a batch's time scales with 1 / SMs; small graphs, whose batches
+// do not, stay near the minimum.)  On the 8-graph pool of Kronecker 16-25 and
+// uniform 20/23 graphs, whole-GPU batches taking turns measured better in
+// both latency and saturation throughput, so grid_policy 0 is the default.
+constexpr int kMinShareSms = 8;
+constexpr int kReserveSms = 16;
+void set_grid_shares(gbbfs_server* s) {
+  if (s->cfg.grid_policy != 1) return;
+  int count = 0;
+  double wsum = 0;
+  for (const Slot& o : s->slots)
+    if (o.admitted) {
+      count++;
+      wsum += std::sqrt(std::max(1e-3, o.full_batch_ms));
+    }
+  if (count == 0) return;
+  const int sms = s->slots[0].g->sms;
+  const int avail = sms - kReserveSms - kMinShareSms * count;
+  for (Slot& o : s->slots) {
+    if (!o.admitted) continue;
+    int share = 0;   // the whole GPU when there is nothing to split
+    if (count > 1 && avail > 0)
+      share = kMinShareSms +
+              (int)(avail * std::sqrt(std::max(1e-3, o.full_batch_ms)) / wsum);
+    ms_set_grid_sms(o.g, share);
+  }
+}
+
+// Stream priorities by measured batch cost (priorities = 1): the admitted
+// graphs are ranked by their whole-GPU batch time and spread over the
+// device's priority range, the cheapest getting the highest priority, so
+// that when SMs free up the GPU takes a small graph's waiting batch before a
+// large graph's.  Under load this starves the costliest graphs (on the
+// 8-graph pool at 10k queries/s some waited ~1 s), so it is off by default.
+int set_priorities(gbbfs_server* s) {
+  if (s->cfg.priorities != 1) return GBBFS_OK;
+  int least = 0, greatest = 0;
+  GB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  std::vector<size_t> idx;
+  for (size_t i = 0; i < s->slots.size(); i++)
+    if (s->slots[i].admitted) idx.push_back(i);
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
+    return s->slots[a].full_batch_ms < s->slots[b].full_batch_ms;
+  });
+  const int levels = least - greatest + 1;   // greatest is the numerically smaller
+  for (size_t r = 0; r < idx.size(); r++) {
+    Slot& o = s->slots[idx[r]];
+    const int level = idx.size() > 1 ? (int)(r * (size_t)levels / idx.size()) : 0;
+    const int prio = greatest + std::min(level, levels - 1);
+    if (prio == o.priority) continue;
+    GB_TRY(graph_set_stream_priority(o.g, prio));
+    o.priority = prio;
+  }
+  return GBBFS_OK;
+}
+
 // Admission against free HBM and the configured budget; may evict idle slots.
 bool admit(gbbfs_server* s, size_t idx) {
   Slot& sl = s->slots[idx];
@@ -182,6 +254,7 @@ bool admit(gbbfs_server* s, size_t idx) {
                            state_bytes_in_use(s) + need <= s->cfg.hbm_budget_bytes;
     if (hbm_ok && budget_ok) {
       if (ms_prepare(sl.g, 1) != GBBFS_OK) return false;
+      if (ms_set_grid_sms(sl.g, 0) != GBBFS_OK) return false;   // measured on the whole GPU
       // Batching keys, once per graph (k = 0: keys only).
       if (s->cfg.order == 0 && ms_order(sl.g, nullptr, 0, nullptr) != GBBFS_OK) return false;
       // The plain search's cost, once per graph, from the oldest query's
@@ -194,12 +267,16 @@ bool admit(gbbfs_server* s, size_t idx) {
             return false;
           if (sl.plain_ms < 0 || st.device_ms < sl.plain_ms) sl.plain_ms = st.device_ms;
         }
-        // and a 1-source batch's (32 lanes), from its kernel stamps
-        const int32_t src = sl.pending.front().source;
-        if (ms_launch(sl.g, 0, &src, 1) != GBBFS_OK || ms_finish(sl.g, 0) != GBBFS_OK) return false;
-        sl.batch_ms[0] = ms_kernel_ms(sl.g, 0);
       }
+      // A 1-source batch's cost (32 lanes) on the whole GPU, from its kernel
+      // stamps: the batch estimate's start and the weight of the SM split.
+      const int32_t src = sl.pending.front().source;
+      if (ms_launch(sl.g, 0, &src, 1) != GBBFS_OK || ms_finish(sl.g, 0) != GBBFS_OK) return false;
+      sl.full_batch_ms = ms_kernel_ms(sl.g, 0);
+      if (sl.batch_ms[0] < 0) sl.batch_ms[0] = sl.full_batch_ms;
       sl.admitted = true;
+      set_grid_shares(s);
+      if (set_priorities(s) != GBBFS_OK) return false;
       return true;
     }
     if (pass == 1) break;
@@ -216,6 +293,7 @@ bool admit(gbbfs_server* s, size_t idx) {
     msbfs_release(o.g->ms);
     o.g->ms = nullptr;
     o.admitted = false;
+    set_grid_shares(s);
   }
   return false;
 }
@@ -235,6 +313,8 @@ void complete(gbbfs_server* s, Slot& sl, Query& q, const RowStats& rs, int statu
   r.reached = (int64_t)rs.reached;
   r.max_depth = (int32_t)rs.max_depth;
   r.plain = q.plain ? 1 : 0;
+  r.device_begin_ns = q.dev_begin;
+  r.device_end_ns = q.dev_end;
   std::lock_guard<std::mutex> lk(s->mu);
   s->done.push_back(r);
   s->outstanding--;
@@ -252,11 +332,15 @@ void harvest(gbbfs_server* s, Slot& sl) {
       double& est = sl.batch_ms[f.cls];
       if (x > 0) est = est < 0 ? x : (1 - kEwma) * est + kEwma * x;
     }
+    uint64_t dev_begin = 0, dev_end = 0;
+    if (!f.plain && st == GBBFS_OK) ms_kernel_stamps(sl.g, b, &dev_begin, &dev_end);
     const double t = s->now();
     const size_t n = (size_t)sl.g->n;
     for (size_t i = 0; i < f.q.size(); i++) {
       Query& q = f.q[i];
       q.t_done = t;
+      q.dev_begin = dev_begin;
+      q.dev_end = dev_end;
       const RowStats& rs = sl.h_stats[kMsMaxLanes * b + i];
       int qst = st;
       if (qst == GBBFS_OK && f.plain && rs.pad) qst = (int)rs.pad;
@@ -300,9 +384,16 @@ void take_batch(gbbfs_server* s, Slot& sl, size_t lanes, std::vector<Query>& out
 
 // Launch the next batch of a slot into a free buffer.
 void launch(gbbfs_server* s, Slot& sl) {
+  // Batches of one graph on the GPU at once (default 1).  A second batch in
+  // flight only queues behind the first and behind other graphs' batches,
+  // while the queries arriving meanwhile would have joined a later, fuller
+  // batch: on the 8-graph pool at 10k queries/s one in flight gave p50 39 ms
+  // against 65 ms for two, at the same saturation throughput.
+  const int max_inflight = s->cfg.max_inflight > 0 ? s->cfg.max_inflight : 1;
   for (int b = 0; b < 2 && !sl.pending.empty(); b++) {
     Inflight& f = sl.fl[b];
     if (f.busy) continue;
+    if (max_inflight == 1 && sl.fl[b ^ 1].busy) break;
     const int lanes = std::min<int>(ms_lanes(sl.g), std::max(1, s->cfg.max_batch));
     take_batch(s, sl, (size_t)lanes, f.q);
     const int k = (int)f.q.size();
@@ -477,10 +568,14 @@ int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out) {
   if (cfg) s->cfg = *cfg;
   if (s->cfg.max_batch <= 0) s->cfg.max_batch = kMsMaxLanes;
   if ((s->cfg.mode != 0 && s->cfg.mode != 1) || (s->cfg.order != 0 && s->cfg.order != 1) ||
-      (s->cfg.batches_only != 0 && s->cfg.batches_only != 1)) {
+      (s->cfg.batches_only != 0 && s->cfg.batches_only != 1) ||
+      (s->cfg.priorities != 0 && s->cfg.priorities != 1) ||
+      (s->cfg.grid_policy != 0 && s->cfg.grid_policy != 1) || s->cfg.max_inflight < 0 ||
+      s->cfg.max_inflight > 2) {
     delete s;
     last_error() = "server mode must be 0 (batched) or 1 (plain), order 0 (grouped) or 1 "
-                   "(arrival), batches_only 0 or 1";
+                   "(arrival), batches_only 0 or 1, grid_policy 0 or 1, max_inflight 0..2, "
+                   "priorities 0 or 1";
     return GBBFS_ERR_ARG;
   }
   s->t0 = Clock::now();
@@ -530,6 +625,7 @@ int gbbfs_server_submit(gbbfs_server* s, int32_t graph_id, int32_t source, uint8
   q.t_start = q.t_done = 0;
   q.batch = 0;
   q.plain = false;
+  q.dev_begin = q.dev_end = 0;
   s->inbox.push_back(q);
   s->outstanding++;
   if (ticket) *ticket = q.ticket;
@@ -565,6 +661,7 @@ int gbbfs_server_submit_many(gbbfs_server* s, int64_t count, const int32_t* grap
     q.t_start = q.t_done = 0;
     q.batch = 0;
     q.plain = false;
+    q.dev_begin = q.dev_end = 0;
     s->inbox.push_back(q);
     s->outstanding++;
     if (tickets) tickets[i] = q.ticket;

@@ -554,7 +554,9 @@ def msbfs_autotune(g, sample, depth_bytes=1):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("max_batch", ctypes.c_int32),
                 ("hbm_budget_bytes", ctypes.c_int64), ("hbm_reserve_bytes", ctypes.c_int64),
-                ("order", ctypes.c_int32), ("batches_only", ctypes.c_int32)]
+                ("order", ctypes.c_int32), ("batches_only", ctypes.c_int32),
+                ("grid_policy", ctypes.c_int32), ("max_inflight", ctypes.c_int32),
+                ("priorities", ctypes.c_int32)]
 
 
 class Result(ctypes.Structure):
@@ -563,7 +565,8 @@ class Result(ctypes.Structure):
                 ("batch_size", ctypes.c_int32), ("submit_s", ctypes.c_double),
                 ("start_s", ctypes.c_double), ("done_s", ctypes.c_double),
                 ("checksum", ctypes.c_uint64), ("reached", ctypes.c_int64),
-                ("max_depth", ctypes.c_int32), ("plain", ctypes.c_int32)]
+                ("max_depth", ctypes.c_int32), ("plain", ctypes.c_int32),
+                ("device_begin_ns", ctypes.c_uint64), ("device_end_ns", ctypes.c_uint64)]
 
 
 def depth_checksum(depth_u8):
@@ -585,9 +588,9 @@ class Server:
     ARRIVAL = 1
 
     def __init__(self, mode=0, max_batch=256, hbm_budget_bytes=0, hbm_reserve_bytes=0, order=0,
-                 batches_only=0):
+                 batches_only=0, grid_policy=0, max_inflight=0, priorities=0):
         cfg = ServerConfig(mode, max_batch, hbm_budget_bytes, hbm_reserve_bytes, order,
-                           batches_only)
+                           batches_only, grid_policy, max_inflight, priorities)
         h = ctypes.c_void_p()
         _check(lib().gbbfs_server_open(ctypes.byref(cfg), ctypes.byref(h)), "server_open")
         self._h = h
@@ -632,7 +635,9 @@ class Server:
             out.append(dict(ticket=r.ticket, graph_id=r.graph_id, source=r.source,
                             status=r.status, batch_size=r.batch_size, submit_s=r.submit_s,
                             start_s=r.start_s, done_s=r.done_s, checksum=r.checksum,
-                            reached=r.reached, max_depth=r.max_depth, plain=r.plain))
+                            reached=r.reached, max_depth=r.max_depth, plain=r.plain,
+                            device_begin_ns=r.device_begin_ns,
+                            device_end_ns=r.device_end_ns))
         return out
 
     def drain(self, timeout_ms=600000):

@@ -287,6 +287,19 @@ typedef struct gbbfs_server_config {
                                 plain searches when the graph's measured costs
                                 say they take less than one batch; 1: always a
                                 batch                                           */
+  int32_t grid_policy;       /* mode 0: 0 every batch spans the whole GPU (the
+                                graphs' batches take turns); 1 the SMs are split
+                                among the admitted graphs (16 kept for the small
+                                kernels around batches, at least 8 per graph,
+                                the rest by the square root of each graph's
+                                measured batch cost), so the batches of
+                                different graphs run side by side          */
+  int32_t max_inflight;      /* batches of one graph on the GPU at once: 1 or 2
+                                (0 = 1)                                       */
+  int32_t priorities;        /* 0: all graph streams equal; 1: CUDA stream
+                                priorities by measured batch cost, the cheapest
+                                graph first (under load the costliest graphs
+                                can starve: measured, not the default)       */
 } gbbfs_server_config;
 
 typedef struct gbbfs_result {
@@ -302,6 +315,9 @@ typedef struct gbbfs_result {
   int64_t reached;     /* vertices with a depth                                  */
   int32_t max_depth;
   int32_t plain;       /* 1 if a plain single-source search answered it          */
+  /* device clock (%globaltimer, ns) at the start and end of the batch search
+   * kernel that answered it; 0 for a plain search */
+  uint64_t device_begin_ns, device_end_ns;
 } gbbfs_result;
 
 int gbbfs_server_open(const gbbfs_server_config* cfg, gbbfs_server** out);

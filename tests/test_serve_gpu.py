@@ -113,10 +113,17 @@ def test_full_width_batches(native, pool, max_batch, order):
     off, g = pool[2]
     srcs = [int(s) for s in native.pick_sources(off, 40)]
     exp = {s: u8(native.DOBFS(g, s, depth=True)[1]) for s in srcs}
-    keys = [(0, srcs[i % len(srcs)]) for i in range(2 * max_batch + 150)]
+    picks = np.array([srcs[i % len(srcs)] for i in range(2 * max_batch + 150)], np.int32)
     with native.Server(mode=0, max_batch=max_batch, order=order) as srv:
         srv.add_graph(g)
-        res, _ = run_queries(native, srv, keys, [g.n], False)
+        srv.submit(0, srcs[0])                  # admission first
+        srv.drain()
+        srv.poll(16)
+        # one burst: the batcher sees every query before it fills lanes
+        srv.submit_many(np.zeros(len(picks), np.int32), picks)
+        srv.drain()
+        res = srv.poll(4096)
+        assert len(res) == len(picks)
         assert max(r["batch_size"] for r in res) == max_batch
         for r in res:
             assert r["status"] == 0
@@ -239,3 +246,39 @@ def test_plain_or_batch_per_launch(native, pool, batches_only):
         else:
             assert plain and all(r["batch_size"] < 256 for r in plain)
         assert max(r["batch_size"] for r in res) > 32
+
+
+def test_batches_of_two_graphs_overlap_on_the_device(native):
+    """With the SMs split among the graphs (grid_policy 1), the batches of two
+    graphs run on the GPU at the same time: some pair of their device-clock
+    intervals overlaps.  Every result still equals the single-source search."""
+    specs = [(18, False), (17, True)]
+    graphs = []
+    try:
+        for sc, uni in specs:
+            graphs.append(native.Graph.from_edges(native.generate_edges(sc, 16, uni)))
+        srcs = [native.pick_sources(g.offsets, 64) for g in graphs]
+        with native.Server(mode=0, batches_only=1, max_batch=32, grid_policy=1) as srv:
+            for g in graphs:
+                srv.add_graph(g)
+            gids = np.repeat(np.arange(2, dtype=np.int32), 512)
+            picks = np.concatenate([srcs[i][np.arange(512) % 64] for i in range(2)])
+            order = np.random.default_rng(3).permutation(len(gids))
+            srv.submit_many(gids[order], picks[order])
+            srv.drain()
+            res = srv.poll(4096)
+        assert len(res) == 1024 and all(r["status"] == 0 for r in res)
+        iv = [sorted({(r["device_begin_ns"], r["device_end_ns"]) for r in res
+                      if r["graph_id"] == gid}) for gid in range(2)]
+        assert all(len(x) >= 2 and all(b > a > 0 for a, b in x) for x in iv)
+        overlaps = sum(1 for a0, a1 in iv[0] for b0, b1 in iv[1] if a0 < b1 and b0 < a1)
+        assert overlaps > 0, iv
+        for gid, g in enumerate(graphs):
+            for s in srcs[gid][:8]:
+                d = u8(native.DOBFS(g, int(s), depth=True)[1])
+                want = native.depth_checksum(d)
+                got = {r["checksum"] for r in res if r["graph_id"] == gid and r["source"] == s}
+                assert got == {want}
+    finally:
+        for g in graphs:
+            g.close()
