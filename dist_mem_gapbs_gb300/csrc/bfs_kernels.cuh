@@ -450,6 +450,11 @@ __global__ void __launch_bounds__(kThreads) k_td(Bufs<OffT> b) {
 // sweep that follows (k_b2q<OffT, true>) turns the bitmap into the next queue
 // in vertex order, with degree prefix, packed counter and visited update, so
 // the step's count and scout_count are the reference's exactly.
+#ifndef GBBFS_TDB_GROUP
+#define GBBFS_TDB_GROUP 8
+#endif
+constexpr int kTdbGroup = GBBFS_TDB_GROUP;   // ordinary chunks in flight per warp
+
 template <typename OffT>
 __global__ void __launch_bounds__(kThreads) k_tdb(Bufs<OffT> b) {
   DevState* st = b.st;
@@ -495,18 +500,19 @@ __global__ void __launch_bounds__(kThreads) k_tdb(Bufs<OffT> b) {
     uint64_t sj = ~0ull;
     int32_t uj = 0;
     uint64_t rj = 0;
-    for (uint64_t c = c_begin; c < c_end; c++, e0 += 32) {
-      if (ij != i0 + lane) {
-        ij = i0 + lane;
-        sj = ~0ull;
-        uj = 0;
-        rj = 0;
-        if (ij < F) {
-          sj = (uint64_t)qs[ij];
-          uj = qv[ij];
-          rj = (uint64_t)off[uj];
-        }
+    auto reload = [&]() {
+      ij = i0 + lane;
+      sj = ~0ull;
+      uj = 0;
+      rj = 0;
+      if (ij < F) {
+        sj = (uint64_t)qs[ij];
+        uj = qv[ij];
+        rj = (uint64_t)off[uj];
       }
+    };
+    for (uint64_t c = c_begin; c < c_end;) {
+      if (ij != i0 + lane) reload();
       const uint64_t s_next = shfl(sj, 1);
       if (c + kHub <= c_end && s_next >= e0 + 32 * kHub) {
         const int32_t u = __shfl_sync(kFull, uj, 0);
@@ -519,24 +525,59 @@ __global__ void __launch_bounds__(kThreads) k_tdb(Bufs<OffT> b) {
         for (int q = 0; q < kHub; q++)
           if (v[q] >= 0) visit(v[q], u);
         if (s_next == e0 + 32 * kHub) i0 += 1;
-        c += kHub - 1;
-        e0 += 32 * (kHub - 1);
+        c += kHub;
+        e0 += 32 * kHub;
         continue;
       }
-      unsigned mybit = 0;
-      if (lane == 0) mybit = 1u;
-      else if (ij < F && sj < e0 + 32) mybit = 1u << (unsigned)(sj - e0);
-      const unsigned starts = __reduce_or_sync(kFull, mybit);
-      const int k = __popc(starts & (kFull >> (31 - lane))) - 1;
-      const int32_t u = __shfl_sync(kFull, uj, k);
-      const uint64_t s = shfl(sj, k);
-      const uint64_t r = shfl(rj, k);
-      const uint64_t e = e0 + lane;
-      if (e < E) visit(__ldg(nbr + (r + (e - s))), u);
-      const unsigned le = __ballot_sync(kFull, lane == 0 || (ij < F && sj <= e0 + 32));
-      int adv = __popc(le) - 1;
-      if (le == kFull && i0 + 32 < F && (uint64_t)qs[i0 + 32] == e0 + 32) adv = 32;
-      i0 += adv;
+      // Up to kTdbGroup chunks of ordinary entries: each mapped to its queue
+      // entries through the window first (the window is reloaded when the
+      // walk moved past it), then all their neighbour loads issued together,
+      // then all their bitmap tests, so a warp keeps several chunks' loads in
+      // flight instead of one.
+      int32_t gu[kTdbGroup];
+      uint64_t gi[kTdbGroup];
+      bool gv[kTdbGroup];
+#pragma unroll
+      for (int t = 0; t < kTdbGroup; t++) {
+        gv[t] = false;
+        gu[t] = 0;
+        gi[t] = 0;
+        if (c < c_end) {
+          if (t > 0 && ij != i0 + lane) reload();
+          unsigned mybit = 0;
+          if (lane == 0) mybit = 1u;
+          else if (ij < F && sj < e0 + 32) mybit = 1u << (unsigned)(sj - e0);
+          const unsigned starts = __reduce_or_sync(kFull, mybit);
+          const int k = __popc(starts & (kFull >> (31 - lane))) - 1;
+          gu[t] = __shfl_sync(kFull, uj, k);
+          const uint64_t sk = shfl(sj, k);
+          const uint64_t rk = shfl(rj, k);
+          const uint64_t e = e0 + lane;
+          gv[t] = e < E;
+          gi[t] = rk + (e - sk);
+          const unsigned le = __ballot_sync(kFull, lane == 0 || (ij < F && sj <= e0 + 32));
+          int adv = __popc(le) - 1;
+          if (le == kFull && i0 + 32 < F && (uint64_t)qs[i0 + 32] == e0 + 32) adv = 32;
+          i0 += adv;
+          c++;
+          e0 += 32;
+        }
+      }
+      int32_t v[kTdbGroup];
+#pragma unroll
+      for (int t = 0; t < kTdbGroup; t++) v[t] = gv[t] ? __ldg(nbr + gi[t]) : -1;
+      uint32_t w[kTdbGroup];
+#pragma unroll
+      for (int t = 0; t < kTdbGroup; t++)
+        w[t] = v[t] >= 0 ? (__ldcg(visited + (v[t] >> 5)) | __ldcg(claim + (v[t] >> 5))) : kFull;
+#pragma unroll
+      for (int t = 0; t < kTdbGroup; t++) {
+        if (v[t] >= 0 && !(w[t] & (1u << (v[t] & 31)))) {
+          atomicOr(claim + (v[t] >> 5), 1u << (v[t] & 31));
+          parent[v[t]] = gu[t];
+          if (depth) depth[v[t]] = level;
+        }
+      }
     }
   }
   stamp_end(st);
