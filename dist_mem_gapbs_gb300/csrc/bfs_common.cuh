@@ -75,6 +75,7 @@ template <typename OffT>
 struct Bufs {
   const OffT* off;
   const int32_t* nbr;
+  const int2* head;   // first two neighbours per vertex, or null
   const uint32_t* iso;
   uint32_t* visited;
   uint32_t* bm0;

@@ -73,6 +73,7 @@ void release(gbbfs_graph* g) {
   if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->off);
   cudaFree(g->nbr);
+  cudaFree(g->head);
   cudaFree(g->iso);
   cudaFree(g->visited);
   cudaFree(g->bm[0]);
@@ -110,6 +111,7 @@ Bufs<OffT> bufs(const gbbfs_graph* g) {
   Bufs<OffT> b;
   b.off = reinterpret_cast<const OffT*>(g->off);
   b.nbr = g->nbr;
+  b.head = g->head;
   b.iso = g->iso;
   b.visited = g->visited;
   b.bm0 = g->bm[0];
@@ -170,6 +172,9 @@ int upload(gbbfs_graph* g, const int64_t* offsets, const int32_t* neigh) {
   k_iso_mask<OffT><<<g->sms * 8, kThreads, 0, g->stream>>>(
       g->n, g->W, reinterpret_cast<const OffT*>(g->off), g->iso);
   GB_CUDA(cudaGetLastError());
+  k_heads<OffT><<<g->sms * 8, kThreads, 0, g->stream>>>(
+      g->n, reinterpret_cast<const OffT*>(g->off), g->nbr, g->head);
+  GB_CUDA(cudaGetLastError());
   GB_CUDA(cudaStreamSynchronize(g->stream));
   return setup_grids<OffT>(g);
 }
@@ -193,7 +198,7 @@ int create(const int64_t* offsets, const int32_t* neigh, int64_t n, int64_t m,
   }
   const size_t offsz = g->off32 ? 4 : 8;
   // Admission: everything this handle allocates, against free HBM.
-  const size_t need = offsz * (n + 1) + 4 * (size_t)m + 4 * 4 * (size_t)g->W +
+  const size_t need = offsz * (n + 1) + 4 * (size_t)m + 8 * (size_t)n + 4 * 4 * (size_t)g->W +
                       2 * 4 * 32 * (size_t)g->W + 2 * (4 + offsz) * (size_t)(n + 1) +
                       8 * (n + 1) + sizeof(DevState) + (64 << 20);
   size_t free_b = 0, total_b = 0;
@@ -212,6 +217,7 @@ int create(const int64_t* offsets, const int32_t* neigh, int64_t n, int64_t m,
     GB_TRY(dev_alloc(g, reinterpret_cast<unsigned long long**>(&g->off), n + 1));
   }
   GB_TRY(dev_alloc(g, &g->nbr, (size_t)m));
+  GB_TRY(dev_alloc(g, &g->head, (size_t)n));
   GB_TRY(dev_alloc(g, &g->iso, g->W));
   GB_TRY(dev_alloc(g, &g->visited, g->W));
   GB_TRY(dev_alloc(g, &g->bm[0], g->W));

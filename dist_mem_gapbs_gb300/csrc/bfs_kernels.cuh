@@ -647,6 +647,7 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
   uint32_t* __restrict__ next = kParity ? b.bm0 : b.bm1;
   const OffT* __restrict__ off = b.off;
   const int32_t* __restrict__ nbr = b.nbr;
+  const int2* __restrict__ heads = kBatchFirst == 2 ? b.head : nullptr;
   uint32_t* __restrict__ visited = b.visited;
   int32_t* __restrict__ parent = st->parent;
   const int64_t W = b.W;
@@ -681,6 +682,7 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
     int item = -1;           // chunk-local index of my vertex, -1 when idle
     uint64_t pos = 0, end = 0, start = 0;
     uint32_t lim = kBatchFirst;   // neighbours of this round
+    int2 hd = make_int2(-1, -1);  // its neighbour heads (first round)
     for (;;) {
       const unsigned needy = __ballot_sync(kFull, item < 0);
       if (item < 0) {
@@ -690,6 +692,7 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
           const int64_t u = ((base + (item >> 5)) << 5) + (item & 31);
           start = pos = (uint64_t)off[u];
           end = (uint64_t)off[u + 1];
+          if (heads) hd = __ldg(heads + u);
           lim = kBatchFirst;
         }
       }
@@ -697,9 +700,16 @@ __global__ void __launch_bounds__(kThreads) k_bu(Bufs<OffT> b) {
       if (!__any_sync(kFull, item >= 0)) break;
       if (item >= 0) {
         int32_t v[kBatch];
+        if (heads && pos == start) {   // first round: the two neighbour heads
+          v[0] = hd.x;
+          v[1] = hd.y;
 #pragma unroll
-        for (int k = 0; k < kBatch; k++)
-          v[k] = (k < (int)lim && pos + k < end) ? __ldg(nbr + pos + k) : -1;
+          for (int k = 2; k < kBatch; k++) v[k] = -1;
+        } else {
+#pragma unroll
+          for (int k = 0; k < kBatch; k++)
+            v[k] = (k < (int)lim && pos + k < end) ? __ldg(nbr + pos + k) : -1;
+        }
         uint32_t hits = 0;
 #pragma unroll
         for (int k = 0; k < kBatch; k++)
@@ -839,6 +849,20 @@ __global__ void k_narrow_offsets(const int64_t* __restrict__ in, OffT* __restric
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x)
     out[i] = (OffT)in[i];
+}
+
+// head[u] = (first, second) neighbour of u in sorted order, -1 past its
+// degree: the bottom-up step's first round of probes reads these 8 bytes,
+// which lie next to those of the vertices the warp's other lanes take,
+// instead of a 32-byte sector of nbr per vertex.
+template <typename OffT>
+__global__ void k_heads(int64_t n, const OffT* __restrict__ off, const int32_t* __restrict__ nbr,
+                        int2* __restrict__ head) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t a = (uint64_t)off[u], e = (uint64_t)off[u + 1];
+    head[u] = make_int2(a < e ? nbr[a] : -1, a + 1 < e ? nbr[a + 1] : -1);
+  }
 }
 
 // iso bit = degree 0 or id >= n: never visited, never scanned.

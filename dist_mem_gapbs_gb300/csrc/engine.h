@@ -107,6 +107,7 @@ struct gbbfs_graph {
   int sms = 0;
   void* off = nullptr;      // uint32_t* or unsigned long long*
   int32_t* nbr = nullptr;
+  int2* head = nullptr;     // first two neighbours of every vertex (-1 past its degree)
   uint32_t* iso = nullptr;
   uint32_t* visited = nullptr;
   uint32_t* bm[2] = {nullptr, nullptr};

@@ -171,6 +171,7 @@ int gbbfs_bfs_noalloc(const int64_t* d_offsets, const int32_t* d_neigh, int64_t 
   Bufs<OffT> b;
   b.off = reinterpret_cast<const OffT*>(d_offsets);
   b.nbr = d_neigh;
+  b.head = nullptr;   // no room for the neighbour heads: first probes read nbr
   b.iso = reinterpret_cast<uint32_t*>(base + kOffIso);
   b.visited = reinterpret_cast<uint32_t*>(base + kOffVisited);
   b.bm0 = reinterpret_cast<uint32_t*>(base + kOffBm0);
