@@ -164,6 +164,32 @@ def step_alg_bytes(n, step, prev_count):
     return n // 8 + 4 * step["count"]
 
 
+def step_layout_bytes(n, step, prev_count):
+    """Bytes one step must move between HBM and the SMs with this build's
+    layout (the frontier bitmaps, 8 MB at scale 26, stay in L2 and are not
+    counted): uint32 offsets, 32-bit bitmaps swept instead of a parent sweep,
+    parents written once per claim."""
+    W4 = 4 * ((n + 31) // 32)                  # one bitmap, in bytes
+    k, cnt = step["kind"], step["count"]
+    if k == "td":
+        b = 12 * prev_count + 4 * step["edges"] + 4 * cnt + 16 * cnt
+        if step["edges"] > (n >> 3):           # k_tdb + sweep: claim bitmap swept
+            b += 2 * W4
+        return b
+    if k == "bu":
+        return 2 * W4 + 4 * min(cnt, W4 // 4) + 4 * step["unvisited"] + 4 * step["edges"] + 4 * cnt
+    if k == "e":
+        return 4 * cnt
+    return W4 + 16 * cnt
+
+
+def init_layout_bytes(n):
+    """k_init: the -1 fill of parent (4 bytes per vertex slot), the iso
+    bitmap read, visited and the first frontier bitmap written."""
+    W = (n + 31) // 32
+    return 4 * 32 * W + 3 * 4 * W
+
+
 def load_fixture(graph):
     """The reference's own results for this workload (tests/golden/golden_large.json),
     or None when the workload has no fixture."""
@@ -414,17 +440,20 @@ def run_gbbfs(args):
     # the library's stream.
     kind_time = {"init": 0.0, "td": 0.0, "bu": 0.0, "e": 0.0, "c": 0.0}
     kind_bytes = {"init": 0, "td": 0, "bu": 0, "e": 0, "c": 0}
+    kind_layout = {"init": 0, "td": 0, "bu": 0, "e": 0, "c": 0}
     kind_launch = {"init": 0, "td": 0, "bu": 0, "e": 0, "c": 0}
     stepped = []
     one_step(stepped, stepped=True)
     for s, st in stepped:
         kind_time["init"] += st.init_seconds
         kind_bytes["init"] += 12 * n
+        kind_layout["init"] += init_layout_bytes(n)
         kind_launch["init"] += 1
         prev = 1
         for step, ref in zip(st.steps, info[s]["steps"]):
             kind_time[step["kind"]] += step["seconds"]
             kind_bytes[step["kind"]] += step_alg_bytes(n, ref, prev)
+            kind_layout[step["kind"]] += step_layout_bytes(n, ref, prev)
             kind_launch[step["kind"]] += 1
             prev = ref["count"]
     kernel_names = {"init": "k_init", "td": "k_td", "bu": "k_bu", "e": "k_q2b", "c": "k_b2q"}
@@ -474,6 +503,21 @@ def run_gbbfs(args):
                "sample": "%d sources of the workload, oracle port of the reference's OpenMP "
                          "DOBFS" % len(c_secs)}
         share = {k: kind_time[k] / max(1e-12, sum(kind_time.values())) for k in kind_time}
+        t_all = sum(kind_time.values())
+        searches = max(1, len(stepped))
+
+        def frac_of(bytes_total, t):
+            return bytes_total / t / 1e9 / peak if t > 0 else 0.0
+        whole = {
+            "note": "all step kernels of the host-stepped pass: bytes / device time",
+            "device_ms_per_search": 1e3 * t_all / searches,
+            "model_bytes_per_search": sum(kind_bytes.values()) / searches,
+            "model_frac": frac_of(sum(kind_bytes.values()), t_all),
+            "layout_bytes_per_search": sum(kind_layout.values()) / searches,
+            "layout_frac": frac_of(sum(kind_layout.values()), t_all),
+            "per_kernel_layout_frac": {kernel_names[k]: frac_of(kind_layout[k], kind_time[k])
+                                       for k in kind_time if kind_time[k] > 0},
+        }
         line = {
             "metric": "GTEPS (harmonic mean over sources)", "value": value, "unit": "GTEPS",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -486,6 +530,7 @@ def run_gbbfs(args):
                          "alg_bytes_per_launch": kind_bytes[dom] / max(1, kind_launch[dom]),
                          "launch_ms": 1e3 * kind_time[dom] / max(1, kind_launch[dom])},
             "kernel_share": share,
+            "whole_search_roofline": whole,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_total, "unit": "GTEPS", "h2d_bytes_per_step": 4 * len(sources),
                     "d2h_bytes_per_step": 4 * n * len(sources)},
