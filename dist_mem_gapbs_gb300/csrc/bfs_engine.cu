@@ -130,6 +130,14 @@ Bufs<OffT> bufs(const gbbfs_graph* g) {
   return b;
 }
 
+// The sweep after a bitmap top-down step: the shared-memory tile version for
+// 32-bit offsets, the per-vertex-load version otherwise.
+template <typename OffT>
+const void* sweep_kernel() {
+  if constexpr (sizeof(OffT) == 4) return (const void*)k_sweep<OffT>;
+  else return (const void*)k_b2q<OffT, true>;
+}
+
 int occupancy_grid(const void* fn, int sms, int* grid) {
   int per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
@@ -145,6 +153,7 @@ int setup_grids(gbbfs_graph* g) {
   GB_TRY(occupancy_grid((const void*)k_q2b<OffT>, g->sms, &g->grid_q2b));
   GB_TRY(occupancy_grid((const void*)k_b2q<OffT, false>, g->sms, &g->grid_b2q));
   GB_TRY(occupancy_grid((const void*)k_tdb<OffT>, g->sms, &g->grid_tdb));
+  GB_TRY(occupancy_grid(sweep_kernel<OffT>(), g->sms, &g->grid_sweep));
   return GBBFS_OK;
 }
 
@@ -306,8 +315,8 @@ int build_graph(gbbfs_graph* g) {
   cudaGraphNode_t tdb;
   GB_TRY(add_kernel(&tdb, sp.conditional.phGraph_out[kSelTDB], nullptr, 0,
                     (const void*)k_tdb<OffT>, g->grid_tdb, kThreads, args_b));
-  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelTDB], &tdb, 1,
-                    (const void*)k_b2q<OffT, true>, g->grid_b2q, kThreads, args_b));
+  GB_TRY(add_kernel(&k, sp.conditional.phGraph_out[kSelTDB], &tdb, 1, sweep_kernel<OffT>(),
+                    g->grid_sweep, kThreads, args_b));
 
   cudaGraphNode_t copy_node;
   GB_CUDA(cudaGraphAddMemcpyNode1D(&copy_node, graph, &loop_node, 1, g->h_st, g->st,
@@ -412,10 +421,13 @@ int run_stepped(gbbfs_graph* g, std::vector<double>* kernel_seconds) {
     GB_TRY(step_event(g, 2 * steps));
     switch (kind) {
       case kKindTD: k_td<OffT><<<g->grid_td, kThreads, 0, s>>>(b); break;
-      case kKindTDB:
+      case kKindTDB: {
         k_tdb<OffT><<<g->grid_tdb, kThreads, 0, s>>>(b);
-        k_b2q<OffT, true><<<g->grid_b2q, kThreads, 0, s>>>(b);
+        void* args[] = {&b};
+        GB_CUDA(cudaLaunchKernel(sweep_kernel<OffT>(), dim3(g->grid_sweep), dim3(kThreads), args,
+                                 0, s));
         break;
+      }
       case kKindE: k_q2b<OffT><<<g->grid_q2b, kThreads, 0, s>>>(b); break;
       case kKindBU:
         if (g->h_st->parity)

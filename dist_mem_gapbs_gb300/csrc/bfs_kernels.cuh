@@ -842,6 +842,90 @@ __global__ void __launch_bounds__(kThreads) k_b2q(Bufs<OffT> b) {
 }
 
 // ---------------------------------------------------------------------------
+// The sweep after k_tdb, for 32-bit offsets: the same result as
+// k_b2q<OffT, true> (claims to the next queue in vertex order with their
+// degree prefix, claim bitmap cleared, visited updated), for the dense claim
+// bitmaps such steps leave.  A CTA takes 256 bitmap words (8192 vertices) at
+// a time and first copies their 8193 offsets into shared memory with
+// coalesced loads; each thread then reads the degrees of its word's claimed
+// vertices from there, instead of a chain of two random offset loads per
+// claimed vertex, twice.  (The copy is skipped for a tile without claims.)
+constexpr int kSweepOffs = kThreads * 32 + 1;
+__device__ __forceinline__ int sweep_slot(int i) { return (i >> 5) * 33 + (i & 31); }
+
+template <typename OffT>
+__global__ void __launch_bounds__(kThreads) k_sweep(Bufs<OffT> b) {
+  static_assert(sizeof(OffT) == 4, "the shared tile holds 32-bit offsets");
+  __shared__ OffT so[kThreads * 33 + 1];   // padded: thread t's 33 offsets at t*33
+  __shared__ unsigned long long warp_tot[kWarpsPerCta];
+  __shared__ unsigned long long cta_base;
+  DevState* st = b.st;
+  const int dst = st->cur ^ 1;
+  uint32_t* claim = st->parity ? b.bm1 : b.bm0;
+  int32_t* qv_out = dst ? b.qv1 : b.qv0;
+  OffT* qs_out = dst ? b.qs1 : b.qs0;
+  const OffT* __restrict__ off = b.off;
+  const int shift = b.shift;
+  const int64_t W = b.W, n = b.n;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const unsigned long long emask = (1ull << shift) - 1;
+  const int64_t span = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t w0 = (int64_t)blockIdx.x * blockDim.x; w0 < W; w0 += span) {
+    const int64_t w = w0 + threadIdx.x;
+    uint32_t bits = 0;
+    if (w < W) {
+      bits = claim[w];
+      if (bits) {
+        claim[w] = 0;
+        b.visited[w] |= bits;
+      }
+    }
+    if (!__syncthreads_or(bits != 0)) continue;
+    const int64_t v0 = w0 << 5;
+    for (int i = threadIdx.x; i < kSweepOffs; i += kThreads) {
+      const int64_t v = v0 + i;
+      so[sweep_slot(i)] = off[v < n ? v : n];   // ids past n: degree 0
+    }
+    __syncthreads();
+    const int t0 = threadIdx.x << 5;
+    unsigned long long degsum = 0;
+    for (uint32_t x = bits; x; x &= x - 1) {
+      const int j = __ffs(x) - 1;
+      degsum += (unsigned long long)(so[sweep_slot(t0 + j + 1)] - so[sweep_slot(t0 + j)]);
+    }
+    const unsigned long long mine = ((unsigned long long)__popc(bits) << shift) + degsum;
+    const unsigned long long inc = warp_inclusive_sum(mine, lane);
+    if (lane == 31) warp_tot[wib] = inc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long t = 0;
+      for (int i = 0; i < kWarpsPerCta; i++) {
+        const unsigned long long x = warp_tot[i];
+        warp_tot[i] = t;
+        t += x;
+      }
+      cta_base = t ? atomicAdd(&b.ctr->qpacked[dst], t) : 0;
+    }
+    __syncthreads();
+    if (bits) {
+      const unsigned long long at = cta_base + warp_tot[wib] + inc - mine;
+      uint64_t qpos = at >> shift;
+      uint64_t epos = at & emask;
+      for (uint32_t x = bits; x; x &= x - 1) {
+        const int j = __ffs(x) - 1;
+        qv_out[qpos] = (int32_t)((w << 5) + j);
+        qs_out[qpos] = (OffT)epos;
+        qpos++;
+        epos += (uint64_t)(so[sweep_slot(t0 + j + 1)] - so[sweep_slot(t0 + j)]);
+      }
+    }
+    __syncthreads();
+  }
+  stamp_end(st);
+}
+
+// ---------------------------------------------------------------------------
 // Graph upload helpers.
 template <typename OffT>
 __global__ void k_narrow_offsets(const int64_t* __restrict__ in, OffT* __restrict__ out,

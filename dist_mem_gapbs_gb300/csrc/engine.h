@@ -124,7 +124,8 @@ struct gbbfs_graph {
   std::vector<cudaEvent_t> step_ev;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  int grid_init = 0, grid_td = 0, grid_bu = 0, grid_q2b = 0, grid_b2q = 0, grid_tdb = 0;
+  int grid_init = 0, grid_td = 0, grid_bu = 0, grid_q2b = 0, grid_b2q = 0, grid_tdb = 0,
+      grid_sweep = 0;
   int64_t device_bytes = 0;
   bool have_result = false;
   bool result_depth = false;
