@@ -37,7 +37,7 @@ GRAPHS = {
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbbfs", choices=["gbbfs", "reference"])
     ap.add_argument("--graph", default="g26", choices=sorted(GRAPHS))
@@ -94,17 +94,26 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.skip = 0
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        # nvidia-smi takes a while to start: the timed region opens once its
+        # first sample is in (at most a few seconds' wait); only samples taken
+        # after that are summarised.
+        t_end = time.time() + 5.0
+        while not self.lines and time.time() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.skip = len(self.lines)
         return self
 
     def _read(self):
@@ -123,7 +132,7 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[self.skip:]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 8:
                 continue
@@ -462,18 +471,21 @@ def run_gbbfs(args):
     achieved = kind_bytes[dom] / kind_time[dom] / 1e9 if kind_time[dom] > 0 else 0.0
     traffic = load_traffic(args.graph, kernel_names[dom])
 
-    # End to end through the public call: the sources in, every search's
-    # parent array back in pinned host memory (gbbfs_bfs_many: each copy runs
-    # while the next search does).  Each search is charged an equal share of
-    # the call's wall time.
+    # End to end through the public call: each step is one gbbfs_bfs_many
+    # call over all the sources, the sources in and every search's parent
+    # array back in pinned host memory (each copy runs while the next search
+    # does).  Same warm-up and step count as the device-timed loop; each
+    # search is charged an equal share of the steps' wall time.
     pinned = torch.empty(n, dtype=torch.int32, pin_memory=True)
     host_parent = pinned.numpy()
-    gbbfs.bfs_many(g, sources[:2], host_parent)          # staging arrays allocated
+    for _ in range(args.warmup):
+        gbbfs.bfs_many(g, sources, host_parent)
     t1 = time.perf_counter()
-    gbbfs.bfs_many(g, sources, host_parent)
+    for _ in range(args.steps):
+        gbbfs.bfs_many(g, sources, host_parent)
     e2e_wall = time.perf_counter() - t1
-    e2e_edges = [info[s]["edges"] for s in sources]
-    e2e_secs = [e2e_wall / len(sources)] * len(sources)
+    e2e_edges = [info[s]["edges"] for s in sources] * args.steps
+    e2e_secs = [e2e_wall / len(e2e_edges)] * len(e2e_edges)
     e2e_value = hmean_gteps(e2e_edges, e2e_secs)
 
     parity = None
