@@ -379,7 +379,10 @@ int gbbfs_build_csr(int32_t* el_pairs, int64_t edges, int64_t num_nodes,
  * the format) and Matrix Market ".mtx" coordinate files (src/reader.h:186-256;
  * 1-based, values ignored).  Edge lists must be symmetrized (symmetrize != 0,
  * the -s flag) unless the file says it is symmetric: this engine runs on
- * undirected CSR only. */
+ * undirected CSR only.  Weighted serialized graphs (".wsg") are refused with
+ * GBBFS_ERR_ARG, as the reference's BFS refuses them (its Reader checks that
+ * a serialized file's weightedness matches the graph type,
+ * gapbs-verify/reader.h:254-267). */
 int gbbfs_read_graph(const char* path, int symmetrize, int64_t** offsets_out,
                      int32_t** neigh_out, int64_t* n_out, int64_t* m_dir_out);
 

@@ -217,11 +217,12 @@ def test_edge_list_files_malformed(native, tmp_path):
         with pytest.raises(native.GbbfsError) as e:
             native.make_graph(filename=str(f), symmetrize=True)
         assert e.value.status == native.ERR_IO, name
-    other = tmp_path / "g.txt"
-    other.write_text("0 1\n")
-    with pytest.raises(native.GbbfsError) as e:
-        native.make_graph(filename=str(other), symmetrize=True)
-    assert e.value.status == native.ERR_ARG
+    for name in ("g.txt", "g.wsg"):   # unknown suffix; weighted serialized graph
+        other = tmp_path / name
+        other.write_text("0 1\n")
+        with pytest.raises(native.GbbfsError) as e:
+            native.make_graph(filename=str(other), symmetrize=True)
+        assert e.value.status == native.ERR_ARG, name
     with pytest.raises(native.GbbfsError) as e:
         native.make_graph(filename=str(tmp_path / "missing.el"), symmetrize=True)
     assert e.value.status == native.ERR_IO
