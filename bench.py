@@ -442,7 +442,10 @@ def run_gbbfs(args):
     secs = [st.device_ms * 1e-3 for _, st in records]
     my_value = hmean_gteps(edges, secs)
     busy = sum(secs)
-    launches = sum(1 + 2 * len(st.steps) for _, st in records)  # init + (decide, step) each
+    # init, per step a decide and the step kernel (a top-down step over more
+    # than n/8 frontier edges runs as two: claims, sweep), the final decide
+    launches = sum(2 + sum(3 if (x["kind"] == "td" and x["edges"] > (n >> 3)) else 2
+                           for x in st.steps) for _, st in records)
 
     # Kernel shares and the roofline of the dominant kernel: the same searches
     # once more, host-stepped, with CUDA events around every step kernel on
