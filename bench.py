@@ -192,6 +192,14 @@ def step_layout_bytes(n, step, prev_count):
     return W4 + 16 * cnt
 
 
+def count_launches(step_lists, n):
+    """Kernels the searches launched: init, per step a decide and the step
+    kernel (a top-down step over more than n/8 frontier edges runs as two:
+    claims, sweep), and the final decide that ends the loop."""
+    return sum(2 + sum(3 if (x["kind"] == "td" and x["edges"] > (n >> 3)) else 2
+                       for x in steps) for steps in step_lists)
+
+
 def init_layout_bytes(n):
     """k_init: the -1 fill of parent (4 bytes per vertex slot), the iso
     bitmap read, visited and the first frontier bitmap written."""
@@ -442,10 +450,7 @@ def run_gbbfs(args):
     secs = [st.device_ms * 1e-3 for _, st in records]
     my_value = hmean_gteps(edges, secs)
     busy = sum(secs)
-    # init, per step a decide and the step kernel (a top-down step over more
-    # than n/8 frontier edges runs as two: claims, sweep), the final decide
-    launches = sum(2 + sum(3 if (x["kind"] == "td" and x["edges"] > (n >> 3)) else 2
-                           for x in st.steps) for _, st in records)
+    launches = count_launches([st.steps for _, st in records], n)
 
     # Kernel shares and the roofline of the dominant kernel: the same searches
     # once more, host-stepped, with CUDA events around every step kernel on
