@@ -592,12 +592,25 @@ int gbbfs_server_add_graph(gbbfs_server* s, gbbfs_graph* g, int32_t* graph_id) {
   }
   Slot sl;
   sl.g = g;
-  GB_CUDA(cudaMalloc(&sl.d_stats, sizeof(RowStats) * 2 * kMsMaxLanes));
-  GB_CUDA(cudaHostAlloc(&sl.h_stats, sizeof(RowStats) * 2 * kMsMaxLanes, cudaHostAllocDefault));
-  GB_CUDA(cudaMalloc(&sl.d_plain, std::max<size_t>((size_t)g->n, 256)));
-  GB_CUDA(cudaHostAlloc(&sl.h_par, 2 * kMsMaxLanes * kParBlock, cudaHostAllocDefault));
-  for (int b = 0; b < 2; b++)
-    GB_CUDA(cudaEventCreateWithFlags(&sl.fl[b].done, cudaEventDisableTiming));
+  cudaError_t e = cudaMalloc(&sl.d_stats, sizeof(RowStats) * 2 * kMsMaxLanes);
+  if (e == cudaSuccess)
+    e = cudaHostAlloc(&sl.h_stats, sizeof(RowStats) * 2 * kMsMaxLanes, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaMalloc(&sl.d_plain, std::max<size_t>((size_t)g->n, 256));
+  if (e == cudaSuccess)
+    e = cudaHostAlloc(&sl.h_par, 2 * kMsMaxLanes * kParBlock, cudaHostAllocDefault);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++)
+    e = cudaEventCreateWithFlags(&sl.fl[b].done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    // Give back what this call made; the server keeps its earlier graphs.
+    cudaFree(sl.d_stats);
+    if (sl.h_stats) cudaFreeHost(sl.h_stats);
+    cudaFree(sl.d_plain);
+    if (sl.h_par) cudaFreeHost(sl.h_par);
+    for (int b = 0; b < 2; b++)
+      if (sl.fl[b].done) cudaEventDestroy(sl.fl[b].done);
+    last_error() = std::string("server graph slot: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? GBBFS_ERR_NOMEM : GBBFS_ERR_CUDA;
+  }
   s->slots.push_back(std::move(sl));
   *graph_id = (int32_t)s->slots.size() - 1;
   return GBBFS_OK;
