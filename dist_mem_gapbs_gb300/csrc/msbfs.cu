@@ -406,9 +406,23 @@ int build_order(gbbfs_graph* g, MsState* ms, Alloc&& alloc) {
   return GBBFS_OK;
 }
 
+int build_state(gbbfs_graph* g, int depth_bytes);
+
+// The batched-search state of a graph handle for this depth width: kept when
+// it matches, else built anew.  A build that fails part way is released and
+// detached, so a later call never finds a half-built state.
 int ensure_state(gbbfs_graph* g, int depth_bytes) {
+  if (g->ms && g->ms->depth_bytes == depth_bytes) return GBBFS_OK;
+  const int rc = build_state(g, depth_bytes);
+  if (rc != GBBFS_OK && g->ms) {
+    msbfs_release(g->ms);
+    g->ms = nullptr;
+  }
+  return rc;
+}
+
+int build_state(gbbfs_graph* g, int depth_bytes) {
   MsState* ms = g->ms;
-  if (ms && ms->depth_bytes == depth_bytes) return GBBFS_OK;
   MsConfig keep;
   if (ms) {
     keep = ms->cfg;
