@@ -318,10 +318,6 @@ class Graph:
     def out_degree(self, v):
         return int(self._off[v + 1] - self._off[v])
 
-    @property
-    def offsets(self):
-        return self._off
-
     def device_bytes(self):
         b = ctypes.c_int64()
         _check(lib().gbbfs_graph_info(self.handle, None, None, ctypes.byref(b)), "graph_info")
