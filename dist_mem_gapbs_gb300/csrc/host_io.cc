@@ -108,7 +108,7 @@ int ReadMTX(const std::string& path, std::vector<int32_t>* el, bool* undirected)
     const char* p = lp;
     while (*p == ' ' || *p == '\t') p++;
     if (*p == '%' || *p == '\n' || *p == '\r' || *p == '\0') continue;
-    long long a = 0, b = 0, c = 0;
+    long long a = 0, b = 0;
     char* end = nullptr;
     a = strtoll(p, &end, 10);
     if (end == p) {
@@ -123,8 +123,8 @@ int ReadMTX(const std::string& path, std::vector<int32_t>* el, bool* undirected)
     }
     p = end;
     if (!sized) {
-      c = strtoll(p, &end, 10);
-      if (end == p || a != b) rc = GBBFS_ERR_IO;   // entries count; square only
+      strtoll(p, &end, 10);   // the entry count: present, not used
+      if (end == p || a != b) rc = GBBFS_ERR_IO;   // square only
       sized = true;
       continue;
     }
