@@ -96,9 +96,10 @@ def build_ref(force=False):
     headers = [os.path.join(gv, f) for f in os.listdir(gv) if f.endswith(".h")]
     bfs_drv = os.path.join(HERE, "ref_driver.cc")
     bc_drv = os.path.join(HERE, "ref_bc_driver.cc")
+    sha = os.path.join(HERE, "sha256.h")
     targets = [
-        (os.path.join(REF_OUT, "gapbs_ref"), [bfs_drv, os.path.join(gv, "bfs.cc")], bfs_drv),
-        (os.path.join(REF_OUT, "gapbs_ref_bc"), [bc_drv, os.path.join(gv, "bc.cc")], bc_drv),
+        (os.path.join(REF_OUT, "gapbs_ref"), [bfs_drv, sha, os.path.join(gv, "bfs.cc")], bfs_drv),
+        (os.path.join(REF_OUT, "gapbs_ref_bc"), [bc_drv, sha, os.path.join(gv, "bc.cc")], bc_drv),
         (os.path.join(REF_OUT, "BFS-V"), [os.path.join(gv, "bfs.cc")],
          os.path.join(gv, "bfs.cc")),
     ]

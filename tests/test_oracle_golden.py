@@ -112,3 +112,15 @@ def test_alg_bytes_model(oracle, golden):
             b += n // 8 + 4 * r["claimed"]
         prev = r["claimed"] if r["kind"] != "e" else r["frontier"]
     assert b == st["alg_bytes"]
+
+
+def test_reference_sources_are_found_by_override(tmp_path, monkeypatch):
+    """oracle/build.py looks for the reference's gapbs-verify/ sources in
+    GAPBS_REF_DIR first, then in the staged copy; a directory without them is
+    passed over."""
+    from oracle import build as B
+    (tmp_path / "gapbs-verify").mkdir()
+    monkeypatch.setenv("GAPBS_REF_DIR", str(tmp_path))
+    assert B.ref_dir() != str(tmp_path)          # no bfs.cc yet
+    (tmp_path / "gapbs-verify" / "bfs.cc").write_text("// stand-in\n")
+    assert B.ref_dir() == str(tmp_path)
