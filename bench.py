@@ -174,7 +174,7 @@ def step_alg_bytes(n, step, prev_count):
 
 
 def step_layout_bytes(n, step, prev_count):
-    """Bytes one step must move between HBM and the SMs with this build's
+    """Bytes one step must move between HBM and the SMs with this library's
     layout (the frontier bitmaps, 8 MB at scale 26, stay in L2 and are not
     counted): uint32 offsets, 32-bit bitmaps swept instead of a parent sweep,
     parents written once per claim."""

@@ -15,8 +15,9 @@ graphs, and records:
 
 The large configurations the GPU is measured on (Kronecker-22/24/26 and
 uniform-26, 64 SourcePicker sources each) go to golden_large.json through the
-driver's "fixture" mode: one reference graph build per configuration, the
-hashes computed inside the driver, so no multi-GB array is written out.  The
+reference driver's (oracle/ref_driver.cc) "fixture" mode: one reference graph
+build per configuration, the hashes computed inside that program, so no
+multi-GB array is written out.  The
 same fields are recorded (the depth hash is over the depth the reference's
 parent tree implies).
 
@@ -135,7 +136,7 @@ def main():
 
 
 def parse_fixture(stdout):
-    """graph line, source list and per-trial records of the driver's fixture mode."""
+    """graph line, source list and per-trial records of ref_driver's fixture mode."""
     graph, sources, trials, trace = None, None, [], None
     for line in stdout.splitlines():
         f = line.split()
